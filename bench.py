@@ -1,0 +1,360 @@
+"""Benchmark of the fluid-2d solver step on GB300.
+
+Workload (default): a single 2048x2048-interior grid (2050^2 with boundary), fp32,
+dt 0.05, diffusion = viscosity = 1e-5, 40 diffusion and 40 pressure Jacobi sweeps per
+projection, initial velocity the sum of 64 seeded Gaussian-core vortices, density
+seeded low-frequency noise, no sources. Metric: interior cell-steps per second.
+
+  value     device-resident stepping (fs_step, graph replay), inputs already in HBM;
+            every timed step is bracketed by CUDA events on the solver's stream and
+            L2 is flushed (a 256 MiB write) between timed steps.
+  e2e       the same metric through fs_solve_host() with pinned host buffers: each
+            step uploads the state and sources and downloads the state, like the
+            reference's fluid_solver_gpu::solve.
+  roofline  stencil kernels (the dominant kind): algorithmic bytes per launch (the
+            per-sweep model 12 B/cell/sweep + fused work) over their CUDA-event time
+            in profiled steps, against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle's Jacobi restatement of the same step (OpenMP, all host
+            cores) on a bounded sample.
+
+--impl reference times the reference's own CPU solver algorithm (fluid_solver_cpu,
+restated in the oracle and pinned bit-exactly against the compiled reference) on the
+host cores, single-threaded as the reference is.
+
+Multi-GPU: the path does not shard (one grid per handle); --gpus N runs N
+independent replicas, one per rank, and `value` sums their throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--size", type=int, default=2048, help="interior cells per side")
+    ap.add_argument("--kd", type=int, default=40)
+    ap.add_argument("--kp", type=int, default=40)
+    ap.add_argument("--sweeps", type=int, default=0, help="temporal-blocking depth (0 = default)")
+    ap.add_argument("--tile-rows", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def metric_name():
+    return "cell-steps/s"
+
+
+def workload_config(a, extra=None):
+    cfg = {"workload": f"vortex_field single grid {a.size}x{a.size} interior fp32, dt 0.05, rates 1e-5, "
+                       f"Kd={a.kd} Kp={a.kp} Jacobi sweeps, 64 vortices",
+           "interior": a.size, "kd": a.kd, "kp": a.kp, "l2": "flushed between timed steps (256 MiB write)",
+           "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            j = json.loads(p.read_text())
+            return float(j["hbm_gbs"]), "measured"
+        except (ValueError, KeyError):
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(w, kd, kp, budget_s=15.0):
+    """The oracle's Jacobi restatement (same arithmetic as the CUDA path), OpenMP over
+    all host cores, timed on whole steps until about budget_s seconds elapse."""
+    import oracle
+
+    cores = os.cpu_count() or 1
+    d, u, v = w.state()
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        d, u, v = oracle.gpu_solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt, kd=kd, kp=kp)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 20:
+            break
+    el = time.perf_counter() - t0
+    return {"value": w.interior_cells * steps / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} whole steps of the {w.rows - 2}^2 workload, oracle Jacobi restatement of "
+                      f"fluid_solver_gpu.cu, OpenMP {cores} threads, {el:.1f} s"}
+
+
+def run_reference(a):
+    """Reference arm: fluid_solver_cpu (Gauss-Seidel) restated in the oracle and pinned
+    bit-exactly against the compiled reference; single-threaded like the reference."""
+    import oracle
+    from fluid2d_gb300 import workloads
+
+    rank, world, _ = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return
+    size = a.size
+    w = workloads.vortex_field(size, seed=2, kd=a.kd, kp=a.kp)
+    d, u, v = w.state()
+    # one probe step sets the sample size so the run stays within a few minutes
+    t0 = time.perf_counter()
+    oracle.cpu_solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt, kd=a.kd, kp=a.kp)
+    per = time.perf_counter() - t0
+    budget = 150.0
+    sample = w
+    if per * (a.steps + a.warmup) > budget:
+        scale = max(64, int(size * (budget / (per * (a.steps + a.warmup))) ** 0.5) // 64 * 64)
+        sample = workloads.vortex_field(scale, seed=2, kd=a.kd, kp=a.kp)
+    d, u, v = sample.state()
+    for _ in range(a.warmup):
+        d, u, v = oracle.cpu_solve(d, sample.ds, sample.diffusion, u, v, sample.us, sample.vs, sample.viscosity,
+                                   sample.dt, kd=a.kd, kp=a.kp)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        d, u, v = oracle.cpu_solve(d, sample.ds, sample.diffusion, u, v, sample.us, sample.vs, sample.viscosity,
+                                   sample.dt, kd=a.kd, kp=a.kp)
+    el = time.perf_counter() - t0
+    val = sample.interior_cells * a.steps / el
+    line = {"metric": metric_name(), "value": val, "unit": "cell-steps/s", "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": workload_config(a, {"sample_interior": sample.rows - 2}),
+            "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{a.steps} steps of a {sample.rows - 2}^2 grid (same workload family), "
+                                       "fluid_solver_cpu.cpp restated (Gauss-Seidel), single thread"},
+            "e2e": {"value": val, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_ours(a):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    pkg = __graft_entry__.load_package()
+    from fluid2d_gb300 import build_lib, workloads
+
+    build_lib.build()
+    w = workloads.vortex_field(a.size, seed=2 + rank, kd=a.kd, kp=a.kp)
+    cfg = dict(diffuse_iterations=a.kd, pressure_iterations=a.kp, device=dev, check_finite=0)
+    if a.sweeps:
+        cfg["sweeps_per_pass"] = a.sweeps
+    if a.tile_rows:
+        cfg["tile_rows"] = a.tile_rows
+    s = pkg.Solver(w.rows, w.cols, **cfg)
+    s.upload(*w.state())
+    s.upload_sources(*w.sources())
+    view = s.device_view()
+    stream = torch.cuda.ExternalStream(view.stream, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    # warm-up (also captures the step graph)
+    s.step(w.diffusion, w.viscosity, w.dt, nsteps=max(3, a.warmup))
+    launches0 = s.stats()["kernel_launches"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    clocks = ClockSampler(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        flush_l2()
+        evs[k][0].record(stream)
+        s.step(w.diffusion, w.viscosity, w.dt, nsteps=1, sync=False)
+        evs[k][1].record(stream)
+    s.sync()
+    torch.cuda.synchronize(dev)
+    t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    launches = s.stats()["kernel_launches"] - launches0
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    cells = w.interior_cells
+    value = cells * a.steps * world / (ms / 1e3)
+
+    # per-kernel CUDA-event profile of a few steps (stencil = dominant kind)
+    prof = None
+    for _ in range(a.profile_steps):
+        flush_l2()
+        torch.cuda.synchronize(dev)
+        p = s.profile_step(w.diffusion, w.viscosity, w.dt)
+        if prof is None:
+            prof = p
+        else:
+            for k in prof:
+                for f in ("launches", "ms", "bytes"):
+                    prof[k][f] += p[k][f]
+    peak, peak_kind = measured_peak()
+    st = prof["stencil"]
+    achieved = (st["bytes"] / st["launches"]) / (st["ms"] / st["launches"] / 1e3) / 1e9
+    step_ms_prof = sum(prof[k]["ms"] for k in prof) / a.profile_steps
+    shares = {k: round(prof[k]["ms"] / a.profile_steps / step_ms_prof, 4) for k in prof}
+
+    # end to end through the reference-shaped call with pinned host buffers
+    e2e = None
+    if not a.no_e2e:
+        pins = [pkg.PinnedArray(w.rows, w.cols) for _ in range(6)]
+        for p_, src in zip(pins, (w.d, w.ds, w.u, w.v, w.us, w.vs)):
+            p_.array[...] = src
+        hd, hds, hu, hv, hus, hvs = (p_.array for p_ in pins)
+        e2e_steps = max(3, min(a.steps, 20))
+        for _ in range(2):
+            s.solve(hd, hds, w.diffusion, hu, hv, hus, hvs, w.viscosity, w.dt)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.solve(hd, hds, w.diffusion, hu, hv, hus, hvs, w.viscosity, w.dt)
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        fb = w.rows * w.cols * 4
+        e2e = {"value": cells * e2e_steps * world / el, "unit": "cell-steps/s", "h2d_bytes_per_step": 6 * fb,
+               "d2h_bytes_per_step": 3 * fb, "steps": e2e_steps, "ms_per_step": 1e3 * el / e2e_steps}
+        for p_ in pins:
+            p_.free()
+
+    stats = s.stats()
+    if rank == 0:
+        line = {"metric": metric_name(), "value": value, "unit": "cell-steps/s", "n_gpus": world,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded vortex field)",
+                "config": workload_config(a, {"sweeps_per_pass": stats["sweeps_per_pass"],
+                                              "tile_rows": stats["tile_rows"],
+                                              "launches_per_step": stats["launches_per_step"],
+                                              "passes_per_step": stats["passes_per_step"]}),
+                "gpu_launches": launches,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                             "kernel": "stencil_kernel", "launches_profiled": st["launches"],
+                             "algorithmic_bytes_per_launch": st["bytes"] / st["launches"],
+                             "ms_per_launch": st["ms"] / st["launches"]},
+                "kernel_shares": shares,
+                "step_algorithmic_bytes_per_cell": sum(prof[k]["bytes"] for k in prof) / a.profile_steps / cells,
+                "clocks": clk, "wall_s": t_wall}
+        if e2e:
+            line["e2e"] = e2e
+        if not a.no_cpu and world == 1:
+            line["cpu_baseline"] = cpu_baseline(w, a.kd, a.kp)
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.warmup < 3:
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

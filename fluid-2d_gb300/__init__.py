@@ -1,0 +1,260 @@
+"""fluid2d_gb300 — Python host mirror of the GB300 solver step for mworchel/fluid-2d.
+
+The reference's interface is the C++ class ``fluid_solver`` with one method,
+``solve(density, density_src, diffusion_rate, u, v, u_src, v_src, viscosity, dt)``
+(src/fluid_solver.hpp:16-24), implemented on the GPU by ``fluid_solver_gpu``
+(src/fluid_solver_gpu.cu:222-258). :class:`FluidSolverGPU` mirrors that class over
+the C ABI in ``include/fluid2d_gb300.h``: constructed with ``(rows, cols)``
+including the boundary, ``solve`` updates ``density``, ``u`` and ``v`` in place.
+Arrays are float32 numpy arrays of shape (rows, cols), the reference grid layout.
+
+There is no CPU fallback: every call runs the CUDA library, and importing a handle
+without the built library raises. Build it with ``build_lib.build()`` (or
+``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import build_lib
+
+FS_OK, FS_ERR_ARG, FS_ERR_CUDA, FS_ERR_NONFINITE, FS_ERR_NOT_CONVERGED, FS_ERR_TIMEOUT, FS_ERR_NOMEM, \
+    FS_ERR_STATE = range(8)
+FS_WARM_ZERO, FS_WARM_PREVIOUS = 0, 1
+STAGE_DIFFUSE_DENSITY, STAGE_ADVECT_DENSITY, STAGE_DIFFUSE_VELOCITY, STAGE_PROJECT, STAGE_ADVECT_VELOCITY = 1, 2, 3, 4, 5
+
+LIB_PATH = build_lib.LIB
+
+
+class FluidError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class fs_config(C.Structure):
+    _fields_ = [("rows", C.c_int), ("cols", C.c_int), ("diffuse_iterations", C.c_int),
+                ("pressure_iterations", C.c_int), ("smooth", C.c_int), ("sweeps_per_pass", C.c_int),
+                ("tile_rows", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("warm_start", C.c_int),
+                ("pressure_tolerance", C.c_float), ("pressure_max_iterations", C.c_int),
+                ("check_finite", C.c_int)]
+
+
+class fs_stats(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("kernel_launches", C.c_longlong), ("launches_per_step", C.c_int),
+                ("passes_per_step", C.c_int), ("sweeps_per_pass", C.c_int), ("tile_rows", C.c_int),
+                ("pressure_iterations_last", C.c_int * 2), ("pressure_residual_last", C.c_double * 2),
+                ("nonfinite", C.c_int)]
+
+
+FS_NUM_KINDS = 5
+KIND_NAMES = ("stencil", "splat", "finish", "advect", "memset")
+
+
+class fs_kernel_times(C.Structure):
+    _fields_ = [("launches", C.c_int * FS_NUM_KINDS), ("ms", C.c_double * FS_NUM_KINDS),
+                ("algorithmic_bytes", C.c_double * FS_NUM_KINDS)]
+
+
+class fs_device_view(C.Structure):
+    _fields_ = [("density", C.c_void_p), ("u", C.c_void_p), ("v", C.c_void_p), ("density_source", C.c_void_p),
+                ("u_source", C.c_void_p), ("v_source", C.c_void_p), ("rows", C.c_int), ("cols", C.c_int),
+                ("pitch", C.c_int), ("stream", C.c_void_p)]
+
+
+# Every symbol the C header declares, with its ctypes signature.
+_P = C.c_void_p
+_F = C.c_float
+_I = C.c_int
+SIGNATURES = {
+    "fs_config_init": (C.c_int, [C.POINTER(fs_config), _I, _I]),
+    "fs_create": (C.c_int, [C.POINTER(fs_config), C.POINTER(_P)]),
+    "fs_destroy": (C.c_int, [_P]),
+    "fs_last_error": (C.c_char_p, []),
+    "fs_solve_host": (C.c_int, [_P, _P, _P, _F, _P, _P, _P, _P, _F, _F]),
+    "fs_upload": (C.c_int, [_P, _P, _P, _P]),
+    "fs_upload_sources": (C.c_int, [_P, _P, _P, _P]),
+    "fs_step": (C.c_int, [_P, _F, _F, _F, _I]),
+    "fs_download": (C.c_int, [_P, _P, _P, _P]),
+    "fs_sync": (C.c_int, [_P]),
+    "fs_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
+    "fs_device_view_get": (C.c_int, [_P, C.POINTER(fs_device_view)]),
+    "fs_stage": (C.c_int, [_P, _I, _F, _F]),
+    "fs_profile_step": (C.c_int, [_P, _F, _F, _F, C.POINTER(fs_kernel_times)]),
+    "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
+    "fs_host_free": (C.c_int, [_P]),
+    "fs_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path: str | pathlib.Path | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"fluid2d_gb300: CUDA library not built ({p}); run build_lib.build()")
+    L = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != FS_OK:
+        msg = _lib.fs_last_error().decode() if _lib is not None else ""
+        raise FluidError(rc, msg)
+
+
+def _ptr(a: np.ndarray, writable=False):
+    if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"] or (writable and not a.flags["WRITEABLE"]):
+        raise TypeError("grids must be C-contiguous float32 numpy arrays")
+    return a.ctypes.data
+
+
+def default_config(rows: int, cols: int, **kw) -> fs_config:
+    L = load()
+    cfg = fs_config()
+    _check(L.fs_config_init(C.byref(cfg), rows, cols))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise AttributeError(f"unknown config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Solver:
+    """One grid resident on one GPU (a handle of the C ABI)."""
+
+    def __init__(self, rows: int, cols: int, **config):
+        self._lib = load()
+        self.rows, self.cols = rows, cols
+        self.config = default_config(rows, cols, **config)
+        h = C.c_void_p()
+        _check(self._lib.fs_create(C.byref(self.config), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _shape(self, *arrs):
+        for a in arrs:
+            if a.shape != (self.rows, self.cols):
+                raise ValueError(f"grid shape {a.shape} != ({self.rows}, {self.cols})")
+
+    def upload(self, d, u, v):
+        self._shape(d, u, v)
+        _check(self._lib.fs_upload(self._h, _ptr(d), _ptr(u), _ptr(v)))
+        _check(self._lib.fs_sync(self._h))
+
+    def upload_sources(self, ds, us, vs):
+        self._shape(ds, us, vs)
+        _check(self._lib.fs_upload_sources(self._h, _ptr(ds), _ptr(us), _ptr(vs)))
+        _check(self._lib.fs_sync(self._h))
+
+    def step(self, diffusion_rate, viscosity, dt, nsteps=1, sync=True):
+        _check(self._lib.fs_step(self._h, diffusion_rate, viscosity, dt, nsteps))
+        if sync:
+            _check(self._lib.fs_sync(self._h))
+
+    def stage(self, stage, rate, dt):
+        _check(self._lib.fs_stage(self._h, stage, rate, dt))
+        _check(self._lib.fs_sync(self._h))
+
+    def download(self):
+        d = np.empty((self.rows, self.cols), np.float32)
+        u = np.empty_like(d)
+        v = np.empty_like(d)
+        _check(self._lib.fs_download(self._h, _ptr(d, True), _ptr(u, True), _ptr(v, True)))
+        _check(self._lib.fs_sync(self._h))
+        return d, u, v
+
+    def sync(self):
+        _check(self._lib.fs_sync(self._h))
+
+    def solve(self, density, density_src, diffusion_rate, u, v, u_src, v_src, viscosity, dt):
+        """fluid_solver::solve: one step on host grids, density/u/v updated in place."""
+        self._shape(density, density_src, u, v, u_src, v_src)
+        _check(self._lib.fs_solve_host(self._h, _ptr(density, True), _ptr(density_src), diffusion_rate,
+                                       _ptr(u, True), _ptr(v, True), _ptr(u_src), _ptr(v_src), viscosity, dt))
+
+    def stats(self) -> dict:
+        st = fs_stats()
+        _check(self._lib.fs_get_stats(self._h, C.byref(st)))
+        return {"steps": st.steps, "kernel_launches": st.kernel_launches,
+                "launches_per_step": st.launches_per_step, "passes_per_step": st.passes_per_step,
+                "sweeps_per_pass": st.sweeps_per_pass, "tile_rows": st.tile_rows,
+                "pressure_iterations_last": list(st.pressure_iterations_last),
+                "pressure_residual_last": list(st.pressure_residual_last), "nonfinite": st.nonfinite}
+
+    def profile_step(self, diffusion_rate, viscosity, dt) -> dict:
+        """One eager step with CUDA events around every launch; per kernel kind:
+        launches, milliseconds and algorithmic bytes."""
+        t = fs_kernel_times()
+        _check(self._lib.fs_profile_step(self._h, diffusion_rate, viscosity, dt, C.byref(t)))
+        return {KIND_NAMES[k]: {"launches": t.launches[k], "ms": t.ms[k], "bytes": t.algorithmic_bytes[k]}
+                for k in range(FS_NUM_KINDS)}
+
+    def device_view(self) -> fs_device_view:
+        v = fs_device_view()
+        _check(self._lib.fs_device_view_get(self._h, C.byref(v)))
+        return v
+
+    @property
+    def handle(self):
+        return self._h
+
+
+class FluidSolverGPU(Solver):
+    """Drop-in for the reference's fluid_solver_gpu (src/fluid_solver_gpu.cuh:9-70)."""
+
+    def __init__(self, rows: int, cols: int, **config):
+        super().__init__(rows, cols, **config)
+
+
+class PinnedArray:
+    """A float32 (rows, cols) numpy view of page-locked host memory (fs_host_alloc)."""
+
+    def __init__(self, rows, cols):
+        self._lib = load()
+        p = C.c_void_p()
+        _check(self._lib.fs_host_alloc(C.byref(p), rows * cols * 4))
+        self._p = p
+        buf = (C.c_float * (rows * cols)).from_address(p.value)
+        self.array = np.ctypeslib.as_array(buf).reshape(rows, cols)
+
+    def free(self):
+        if getattr(self, "_p", None):
+            self.array = None
+            self._lib.fs_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,154 @@
+// Semi-Lagrangian advection kernels.
+//
+// Reference behaviour (mworchel/fluid-2d src/fluid_solver_gpu.cu):
+//   density  advect(trace=true) 325-356: D2D copy, memset, advect_trace_kernel
+//            131-162 (forward bilinear splat with fp32 atomicAdd), Neumann fill,
+//            then smooth 314-323 (D2D copy + smooth_kernel 87-97, no fill);
+//   velocity two advect(trace=false) calls 248-251 on copies u0, v0 with
+//            advect_kernel 99-129 (backtrace, clamp, bilinear gather), each followed
+//            by its reflecting fill.
+// Here the density path is three launches with no copies: a memset of the
+// accumulator, the splat, and one "finish" kernel that applies the Neumann fill and
+// the smoothing together. The velocity path is one kernel that backtraces once per
+// cell and gathers u and v together, writing the reflecting edges directly.
+//
+// Operand order and rounding follow the reference expressions; explicit _rn
+// intrinsics keep the compiler from contracting them into FMAs. The splat order of
+// the atomics is unspecified, as in the reference.
+
+#include "fs_internal.cuh"
+
+namespace fs {
+namespace {
+
+__global__ void __launch_bounds__(256) splat_kernel(const float* __restrict__ d0, const float* __restrict__ u,
+                                                    const float* __restrict__ v, float* __restrict__ acc,
+                                                    const AdvectArgs A) {
+    const size_t P = (size_t)A.pitch;
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y + 1; i < A.rows - 1; i += blockDim.y * gridDim.y) {
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j < A.cols - 1; j += blockDim.x * gridDim.x) {
+            const size_t o = (size_t)i * P + j;
+            const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, __ldg(u + o)));
+            const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, __ldg(v + o)));
+            // skipped unless inside [0.5, n-1.5] (fluid_solver_gpu.cu:144); NaN is skipped too
+            if (!(x >= 0.5f && x <= A.xmax && y >= 0.5f && y <= A.ymax)) continue;
+            const int j0 = (int)x, i0 = (int)y;
+            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+            const float d = __ldg(d0 + o);
+            float* t = acc + (size_t)i0 * P + j0;
+            atomicAdd(t, __fmul_rn(__fmul_rn(s1, s3), d));
+            atomicAdd(t + P, __fmul_rn(__fmul_rn(s1, s2), d));
+            atomicAdd(t + 1, __fmul_rn(__fmul_rn(s0, s3), d));
+            atomicAdd(t + P + 1, __fmul_rn(__fmul_rn(s0, s2), d));
+        }
+    }
+}
+
+// Value of the accumulator after set_boundary_continuous (fluid_solver_gpu.cu:11-24):
+// edges read their inner neighbour, corners and the interior read themselves.
+__device__ __forceinline__ float filled(const float* __restrict__ acc, int r, int c, const AdvectArgs& A) {
+    const bool ri = r >= 1 && r <= A.rows - 2, ci = c >= 1 && c <= A.cols - 2;
+    if (ri && !ci) c = (c == 0) ? 1 : A.cols - 2;
+    else if (ci && !ri) r = (r == 0) ? 1 : A.rows - 2;
+    return __ldg(acc + (size_t)r * A.pitch + c);
+}
+
+__global__ void __launch_bounds__(256) density_finish_kernel(const float* __restrict__ acc, float* __restrict__ d,
+                                                             int smooth, const AdvectArgs A, int* nonfinite) {
+    int bad = 0;
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y) {
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x) {
+            float out = filled(acc, i, j, A);
+            if (smooth && i >= 1 && i <= A.rows - 2 && j >= 1 && j <= A.cols - 2) {
+                // 0.2f * (c + l + r + u + d), fluid_solver_gpu.cu:94
+                float s = __fadd_rn(out, filled(acc, i, j - 1, A));
+                s = __fadd_rn(s, filled(acc, i, j + 1, A));
+                s = __fadd_rn(s, filled(acc, i - 1, j, A));
+                s = __fadd_rn(s, filled(acc, i + 1, j, A));
+                out = __fmul_rn(0.2f, s);
+            }
+            d[(size_t)i * A.pitch + j] = out;
+            bad |= !isfinite(out);
+        }
+    }
+    if (bad && nonfinite) atomicOr(nonfinite, 1);
+}
+
+__global__ void __launch_bounds__(256) advect_velocity_kernel(const float* __restrict__ u0,
+                                                              const float* __restrict__ v0, float* __restrict__ u,
+                                                              float* __restrict__ v, const AdvectArgs A) {
+    const size_t P = (size_t)A.pitch;
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y) {
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x) {
+            const bool ri = i >= 1 && i <= A.rows - 2, ci = j >= 1 && j <= A.cols - 2;
+            const size_t o = (size_t)i * P + j;
+            if (!ri && !ci) {  // corners are never written by the reference
+                u[o] = __ldg(u0 + o);
+                v[o] = __ldg(v0 + o);
+                continue;
+            }
+            // Edge cells copy the advected inner neighbour: u is negated on the
+            // left/right edges, v on the top/bottom edges (fluid_solver_gpu.cu:26-54).
+            int si = i, sj = j;
+            float su = 1.f, sv = 1.f;
+            if (!ci) {
+                sj = (j == 0) ? 1 : A.cols - 2;
+                su = -1.f;
+            } else if (!ri) {
+                si = (i == 0) ? 1 : A.rows - 2;
+                sv = -1.f;
+            }
+            const size_t so = (size_t)si * P + sj;
+            // advect_kernel, fluid_solver_gpu.cu:111-126
+            float x = __fsub_rn((float)sj, __fmul_rn(A.dt0, __ldg(u0 + so)));
+            float y = __fsub_rn((float)si, __fmul_rn(A.dt0, __ldg(v0 + so)));
+            x = fmaxf(1.5f, fminf(A.xmax, x));
+            y = fmaxf(1.5f, fminf(A.ymax, y));
+            const int j0 = (int)x, i0 = (int)y;
+            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+            const size_t q = (size_t)i0 * P + j0;
+            const float ua = __ldg(u0 + q), ub = __ldg(u0 + q + 1), uc = __ldg(u0 + q + P), ud = __ldg(u0 + q + P + 1);
+            const float va = __ldg(v0 + q), vb = __ldg(v0 + q + 1), vc = __ldg(v0 + q + P), vd = __ldg(v0 + q + P + 1);
+            const float ut = __fadd_rn(__fmul_rn(s1, ua), __fmul_rn(s0, ub));
+            const float ubm = __fadd_rn(__fmul_rn(s1, uc), __fmul_rn(s0, ud));
+            const float vt = __fadd_rn(__fmul_rn(s1, va), __fmul_rn(s0, vb));
+            const float vbm = __fadd_rn(__fmul_rn(s1, vc), __fmul_rn(s0, vd));
+            u[o] = su * __fadd_rn(__fmul_rn(s3, ut), __fmul_rn(s2, ubm));
+            v[o] = sv * __fadd_rn(__fmul_rn(s3, vt), __fmul_rn(s2, vbm));
+        }
+    }
+}
+
+dim3 grid_for(int rows, int cols) {
+    const int gx = (cols + 31) / 32;
+    int gy = (rows + 7) / 8;
+    // cap the grid (grid-stride loops) at a few waves of 152 SMs x 8 CTAs
+    const long cap = 152L * 8 * 8;
+    if ((long)gx * gy > cap) gy = (int)((cap + gx - 1) / gx);
+    if (gy < 1) gy = 1;
+    return dim3(gx, gy);
+}
+
+}  // namespace
+
+cudaError_t launch_splat(const float* d0, const float* u, const float* v, float* acc, const AdvectArgs& A,
+                         cudaStream_t st) {
+    splat_kernel<<<grid_for(A.rows, A.cols), dim3(32, 8), 0, st>>>(d0, u, v, acc, A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const AdvectArgs& A, int* nonfinite,
+                                  cudaStream_t st) {
+    density_finish_kernel<<<grid_for(A.rows, A.cols), dim3(32, 8), 0, st>>>(acc, d, smooth, A, nonfinite);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
+                                   cudaStream_t st) {
+    advect_velocity_kernel<<<grid_for(A.rows, A.cols), dim3(32, 8), 0, st>>>(u0, v0, u, v, A);
+    return cudaGetLastError();
+}
+
+}  // namespace fs

@@ -1,0 +1,96 @@
+// Internal definitions shared by the solver's CUDA translation units.
+//
+// Storage: every field is a rows x pitch float32 slab in HBM, pitch a multiple of 32
+// floats (128 B) so that each row starts on a 128-byte line; element (i, j) is at
+// i*pitch + j. The reference stores the same fields unpadded (linear_buffer,
+// src/linear_buffer.hpp:34-40: pitch = cols*4 B), which leaves most rows misaligned.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fs {
+
+// Boundary modes of the reference (fluid_solver_gpu.cu:11-54). The sign pair gives
+// the factor applied to the inner neighbour on the left/right edges and on the
+// top/bottom edges; corners are never written.
+enum Bnd : int { BND_CONT = 0, BND_OPP_H = 1, BND_OPP_V = 2 };
+inline __host__ __device__ float bnd_sign_lr(int m) { return m == BND_OPP_H ? -1.f : 1.f; }
+inline __host__ __device__ float bnd_sign_tb(int m) { return m == BND_OPP_V ? -1.f : 1.f; }
+
+// Stencil pass kinds. A diffusion or pressure solve is split into passes; each pass
+// loads a tile with a halo, runs `sweeps` Jacobi sweeps in shared memory and writes
+// the tile back once (temporal blocking).
+enum PassKind : int {
+    PASS_DIFFUSE_FIRST = 0,  // x0 = x + dt*s fused in (add_sources); writes x0
+    PASS_DIFFUSE = 1,        // reads x, x0
+    PASS_PRESSURE_FIRST = 2, // div computed from u, v and written; p starts at 0 (or p_init)
+    PASS_PRESSURE = 3,       // reads p, div
+};
+
+// Region width of the stencil kernels: one column per thread, four warps across.
+constexpr int kRegionW = 128;
+
+struct StencilField {
+    // inputs
+    const float* x;     // state in: x (diffuse), p (pressure; may be null = zero start), u (pressure first)
+    const float* x2;    // sources s (diffuse first) or v (pressure first)
+    const float* cst;   // x0 (diffuse) or div (pressure) for non-first passes
+    // outputs
+    float* y;           // state out (x or p); may be null for a last pressure pass
+    float* cst_out;     // first pass: x0 or div out
+    // gradient-subtract epilogue (last pressure pass): u,v in -> out
+    const float* u_in;
+    const float* v_in;
+    float* u_out;
+    float* v_out;
+    // constants
+    float a, dh, dl, rf;  // diffuse: a and the FP32 pair for 1/(1+4a) (see stencil.cu)
+    float dt;             // add_sources
+    float cdiv;           // divergence factor -0.5f*h
+    float h;              // gradient divisor
+    float s_lr, s_tb;     // boundary signs of this field
+    int kind;             // PassKind
+    int sweeps;           // Jacobi sweeps in this pass
+    int epilogue;         // 1: gradient subtract + velocity fills after the sweeps
+    int halo;             // H: region = tile grown by H on each side
+    int rows, cols, pitch;
+    int tile_w, tile_h, tiles_x, tiles_y, shift_x, shift_y;
+    int tile_begin;       // first block index of this field in the launch
+    int* nonfinite;       // optional flag (epilogue outputs)
+};
+
+constexpr int kMaxStencilFields = 4;
+struct StencilLaunch {
+    StencilField f[kMaxStencilFields];
+    int nfields;
+};
+
+// Semi-Lagrangian advection parameters.
+struct AdvectArgs {
+    int rows, cols, pitch;
+    float dt0;          // sqrt(rows*cols)*dt (fluid_solver_gpu.cu:334)
+    float xmax, ymax;   // cols-1.5f, rows-1.5f
+};
+
+// Tile geometry: tiles partition [0, n) starting at -shift, and never put a domain
+// edge cell (index 0 or n-1) in a different tile from its inner neighbour, so the
+// boundary fill of a tile only ever depends on cells of the same tile.
+inline void tile_split(int n, int tile, int* count, int* shift) {
+    int s = ((n - 1) % tile == 0) ? 1 : 0;
+    *shift = s;
+    *count = (n + s + tile - 1) / tile;
+}
+
+// Launchers (stencil.cu, advect.cu).
+cudaError_t stencil_prepare();
+cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st);
+int stencil_max_halo(int tile_rows);
+cudaError_t launch_splat(const float* d0, const float* u, const float* v, float* acc, const AdvectArgs& A,
+                         cudaStream_t st);
+cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const AdvectArgs& A, int* nonfinite,
+                                  cudaStream_t st);
+cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
+                                   cudaStream_t st);
+
+}  // namespace fs

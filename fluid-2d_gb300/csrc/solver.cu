@@ -1,0 +1,715 @@
+// Solver handle, step orchestration and the C ABI (include/fluid2d_gb300.h).
+//
+// One handle = one grid on one device with one stream. The step is the reference's
+// fluid_solver_gpu::solve (mworchel/fluid-2d src/fluid_solver_gpu.cu:222-258) in the
+// same stage order, planned as a short fixed sequence of fused kernels:
+//
+//   diffuse d,u,v  : ceil(Kd/K) stencil passes, all three fields in each launch
+//                    (add_sources fused into the first pass)
+//   advect d       : memset + forward splat + finish (Neumann fill + smoothing)
+//   project        : ceil(Kp/K) stencil passes (divergence fused into the first,
+//                    gradient subtract + reflecting fills into the last)
+//   advect u,v     : one backtrace kernel for both components
+//   project        : as above
+//
+// K is the temporal-blocking depth (sweeps per HBM pass). The sequence is captured
+// once as a CUDA graph and replayed per step; it is re-captured only when dt or the
+// rates change. The reference instead issues ~190 launches, 94 device copies and a
+// device-wide synchronisation after every kernel per step.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fluid2d_gb300.h"
+#include "fs_internal.cuh"
+
+#define FS_VERSION "0.1.0"
+
+using namespace fs;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(e == cudaErrorMemoryAllocation ? FS_ERR_NOMEM : FS_ERR_CUDA, m);
+}
+
+#define CK(call)                                               \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);    \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (dev < 0) return;
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            if (cudaSetDevice(dev) == cudaSuccess) changed = true;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+enum FieldId { F_D = 0, F_U = 1, F_V = 2 };
+
+}  // namespace
+
+struct fs_solver {
+    fs_config cfg{};
+    int device = 0;
+    int rows = 0, cols = 0, pitch = 0;
+    size_t field_floats = 0;
+    float* slab = nullptr;
+    // state and sources
+    float* st[3] = {};
+    float* src[3] = {};
+    // diffusion scratch per field: x0 and two ping-pong buffers
+    float* x0[3] = {};
+    float* pp[3][2] = {};
+    // advection / projection scratch
+    float* acc = nullptr;
+    float* div = nullptr;
+    float* p[2] = {};
+    float* vel1[2] = {};
+    float* pwarm[2] = {};
+    int* flags = nullptr;  // [0]: non-finite
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_valid = false;
+    float g_diff = 0, g_visc = 0, g_dt = 0;
+    int sweeps = 8;
+    int tile_rows = 64;
+    int launches_per_step = 0;
+    int passes_per_step = 0;
+    bool warm_valid = false;
+    fs_stats stats{};
+    // per-kernel event timing (fs_profile_step); null outside a profiled step
+    fs_kernel_times* prof = nullptr;
+    std::vector<cudaEvent_t> prof_events;
+    std::vector<std::pair<int, double>> prof_marks;  // (kind, algorithmic bytes) per launch
+};
+
+namespace {
+
+// Split `total` sweeps into passes of at most `k` (at least one pass, possibly of
+// zero sweeps, so that fused work such as add_sources always runs).
+std::vector<int> split_sweeps(int total, int k) {
+    int m = std::max(1, (total + k - 1) / k);
+    std::vector<int> out(m, total / m);
+    for (int i = 0; i < total % m; ++i) out[i] += 1;
+    return out;
+}
+
+void set_geometry(StencilField& f, const fs_solver* s, int halo) {
+    f.rows = s->rows;
+    f.cols = s->cols;
+    f.pitch = s->pitch;
+    f.halo = halo;
+    f.tile_w = kRegionW - 2 * halo;
+    f.tile_h = s->tile_rows - 2 * halo;
+    tile_split(s->cols, f.tile_w, &f.tiles_x, &f.shift_x);
+    tile_split(s->rows, f.tile_h, &f.tiles_y, &f.shift_y);
+}
+
+void diffuse_constants(StencilField& f, int rows, int cols, float rate, float dt) {
+    // a = dt * T(rows*cols) * rate in float (fluid_solver_gpu.cu:79)
+    const float a = dt * (float)((size_t)rows * (size_t)cols) * rate;
+    const double D = 1.0 + 4.0 * (double)a;
+    f.a = a;
+    f.dh = (float)D;
+    f.dl = (float)(D - (double)f.dh);
+    f.rf = (float)(1.0 / D);
+}
+
+AdvectArgs advect_args(const fs_solver* s, float dt) {
+    AdvectArgs A;
+    A.rows = s->rows;
+    A.cols = s->cols;
+    A.pitch = s->pitch;
+    // float dt0 = sqrt(m_rows * m_cols) * dt, evaluated in double (fluid_solver_gpu.cu:334)
+    A.dt0 = (float)(std::sqrt((double)((size_t)s->rows * (size_t)s->cols)) * (double)dt);
+    A.xmax = (float)s->cols - 1.5f;
+    A.ymax = (float)s->rows - 1.5f;
+    return A;
+}
+
+float grid_h(int rows, int cols) {
+    // h = 1.0f / sqrtf(m_rows * m_cols) (fluid_solver_gpu.cu:367)
+    return 1.0f / sqrtf((float)((size_t)rows * (size_t)cols));
+}
+
+struct Counter {
+    int launches = 0;
+    int passes = 0;
+};
+
+double interior_cells(const fs_solver* s) { return (double)(s->rows - 2) * (double)(s->cols - 2); }
+
+// Event before a launch (profiled steps only).
+int prof_begin(fs_solver* s) {
+    if (!s->prof) return FS_OK;
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    s->prof_events.push_back(e);
+    CK(cudaEventRecord(e, s->stream));
+    return FS_OK;
+}
+
+// Event after a launch, tagged with its kind and algorithmic bytes.
+int prof_end(fs_solver* s, int kind, double bytes) {
+    if (!s->prof) return FS_OK;
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    s->prof_events.push_back(e);
+    CK(cudaEventRecord(e, s->stream));
+    s->prof_marks.push_back({kind, bytes});
+    return FS_OK;
+}
+
+#define PROF_BEGIN(s)                                 \
+    do {                                              \
+        int rc_ = prof_begin(s);                      \
+        if (rc_ != FS_OK) return rc_;                 \
+    } while (0)
+#define PROF_END(s, kind, bytes)                      \
+    do {                                              \
+        int rc_ = prof_end(s, kind, bytes);           \
+        if (rc_ != FS_OK) return rc_;                 \
+    } while (0)
+
+// Diffusion of a subset of {d, u, v}: add_sources fused into pass 0. Returns the
+// buffer holding each field's result in out[].
+int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates, float dt, float** out,
+                    Counter& cnt) {
+    const std::vector<int> plan = split_sweeps(s->cfg.diffuse_iterations, s->sweeps);
+    const float* cur[3] = {};
+    for (int q = 0; q < nf; ++q) cur[q] = s->st[fields[q]];
+    for (size_t pass = 0; pass < plan.size(); ++pass) {
+        StencilLaunch L{};
+        L.nfields = nf;
+        int begin = 0;
+        for (int q = 0; q < nf; ++q) {
+            const int fid = fields[q];
+            StencilField& f = L.f[q];
+            set_geometry(f, s, plan[pass]);
+            diffuse_constants(f, s->rows, s->cols, rates[q], dt);
+            const int mode = fid == F_D ? BND_CONT : (fid == F_U ? BND_OPP_H : BND_OPP_V);
+            f.s_lr = bnd_sign_lr(mode);
+            f.s_tb = bnd_sign_tb(mode);
+            f.sweeps = plan[pass];
+            f.dt = dt;
+            f.x = cur[q];
+            float* dst = s->pp[fid][pass & 1];
+            f.y = dst;
+            if (pass == 0) {
+                f.kind = PASS_DIFFUSE_FIRST;
+                f.x2 = s->src[fid];
+                f.cst_out = s->x0[fid];
+            } else {
+                f.kind = PASS_DIFFUSE;
+                f.cst = s->x0[fid];
+            }
+            f.tile_begin = begin;
+            begin += f.tiles_x * f.tiles_y;
+            cur[q] = dst;
+        }
+        // per field: 12 B/cell per sweep (read x and x0, write x) + 12 B/cell add_sources
+        const double bytes = nf * interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0));
+        PROF_BEGIN(s);
+        CK(launch_stencil(L, s->tile_rows, s->stream));
+        PROF_END(s, FS_KIND_STENCIL, bytes);
+        cnt.launches++;
+        cnt.passes++;
+    }
+    for (int q = 0; q < nf; ++q) out[q] = const_cast<float*>(cur[q]);
+    return FS_OK;
+}
+
+// project (fluid_solver_gpu.cu:358-404): (u_in, v_in) -> (u_out, v_out). slot picks
+// the warm-start pressure buffer (the two projections of a step keep separate ones).
+int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out, int slot,
+                    Counter& cnt) {
+    const std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
+    const int m = (int)plan.size();
+    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    const float h = grid_h(s->rows, s->cols);
+    const float* pin = (warm && s->warm_valid) ? s->pwarm[slot] : nullptr;
+    for (int pass = 0; pass < m; ++pass) {
+        const bool last = pass == m - 1;
+        StencilLaunch L{};
+        L.nfields = 1;
+        StencilField& f = L.f[0];
+        set_geometry(f, s, plan[pass] + (last ? 1 : 0));
+        f.s_lr = f.s_tb = 1.f;
+        f.sweeps = plan[pass];
+        f.cdiv = -0.5f * h;
+        f.h = h;
+        float* pout = s->p[pass & 1];
+        if (last) pout = warm ? (m == 1 ? s->p[0] : s->pwarm[slot]) : nullptr;
+        if (pass == 0) {
+            f.kind = PASS_PRESSURE_FIRST;
+            f.x = u_in;
+            f.x2 = v_in;
+            f.cst = pin;  // starting pressure (null: zero, as the reference)
+            f.cst_out = s->div;
+        } else {
+            f.kind = PASS_PRESSURE;
+            f.x = s->p[(pass - 1) & 1];
+            f.cst = s->div;
+        }
+        f.y = pout;
+        if (last) {
+            f.epilogue = 1;
+            f.u_in = u_in;
+            f.v_in = v_in;
+            f.u_out = u_out;
+            f.v_out = v_out;
+            f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
+        }
+        // 12 B/cell per sweep (read p and div, write p), + 12 divergence, + 20 gradient
+        const double bytes =
+            interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0) + (last ? 20.0 : 0.0));
+        PROF_BEGIN(s);
+        CK(launch_stencil(L, s->tile_rows, s->stream));
+        PROF_END(s, FS_KIND_STENCIL, bytes);
+        cnt.launches++;
+        cnt.passes++;
+    }
+    if (warm && m == 1) {
+        CK(cudaMemcpyAsync(s->pwarm[slot], s->p[0], s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                           s->stream));
+    }
+    return FS_OK;
+}
+
+int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const float* u, const float* v, float dt,
+                           Counter& cnt) {
+    const AdvectArgs A = advect_args(s, dt);
+    PROF_BEGIN(s);
+    CK(cudaMemsetAsync(s->acc, 0, s->field_floats * sizeof(float), s->stream));
+    PROF_END(s, FS_KIND_MEMSET, 0.0);
+    PROF_BEGIN(s);
+    CK(launch_splat(d0, u, v, s->acc, A, s->stream));
+    PROF_END(s, FS_KIND_SPLAT, 16.0 * interior_cells(s));  // read d0, u, v; write d
+    PROF_BEGIN(s);
+    CK(launch_density_finish(s->acc, d_out, s->cfg.smooth, A, s->cfg.check_finite ? s->flags : nullptr,
+                             s->stream));
+    PROF_END(s, FS_KIND_FINISH, 8.0 * interior_cells(s));  // smooth: read d, write d
+    cnt.launches += 2;
+    return FS_OK;
+}
+
+int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
+    int rc;
+    // density and velocity diffusion are independent; one launch per pass serves all three
+    const int fields[3] = {F_D, F_U, F_V};
+    const float rates[3] = {diff, visc, visc};
+    float* dif[3];
+    if ((rc = enqueue_diffuse(s, fields, 3, rates, dt, dif, cnt)) != FS_OK) return rc;
+    // density: forward advection by the step's initial velocity, then smoothing
+    if ((rc = enqueue_advect_density(s, dif[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt)) != FS_OK) return rc;
+    // velocity: project, advect by itself, project
+    if ((rc = enqueue_project(s, dif[F_U], dif[F_V], s->st[F_U], s->st[F_V], 0, cnt)) != FS_OK) return rc;
+    PROF_BEGIN(s);
+    CK(launch_advect_velocity(s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], advect_args(s, dt), s->stream));
+    PROF_END(s, FS_KIND_ADVECT, 16.0 * interior_cells(s));  // read u0, v0; write u, v
+    cnt.launches++;
+    if ((rc = enqueue_project(s, s->vel1[0], s->vel1[1], s->st[F_U], s->st[F_V], 1, cnt)) != FS_OK) return rc;
+    return FS_OK;
+}
+
+void destroy_graph(fs_solver* s) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->gexec = nullptr;
+    s->graph = nullptr;
+    s->graph_valid = false;
+}
+
+int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
+    int rc;
+    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    for (int k = 0; k < nsteps; ++k) {
+        // The first warm-start step starts from zero pressure; its graph differs.
+        const bool graphable = s->cfg.use_graph && (!warm || s->warm_valid);
+        if (graphable) {
+            if (!s->graph_valid || diff != s->g_diff || visc != s->g_visc || dt != s->g_dt) {
+                destroy_graph(s);
+                Counter cnt;
+                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+                rc = enqueue_step(s, diff, visc, dt, cnt);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+                if (rc != FS_OK) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+                s->graph = g;
+                CK(cudaGraphInstantiate(&s->gexec, g, 0));
+                s->graph_valid = true;
+                s->g_diff = diff;
+                s->g_visc = visc;
+                s->g_dt = dt;
+                s->launches_per_step = cnt.launches;
+                s->passes_per_step = cnt.passes;
+            }
+            CK(cudaGraphLaunch(s->gexec, s->stream));
+            s->stats.kernel_launches += s->launches_per_step;
+        } else {
+            Counter cnt;
+            if ((rc = enqueue_step(s, diff, visc, dt, cnt)) != FS_OK) return rc;
+            s->launches_per_step = cnt.launches;
+            s->passes_per_step = cnt.passes;
+            s->stats.kernel_launches += cnt.launches;
+        }
+        s->warm_valid = true;
+        s->stats.steps++;
+    }
+    return FS_OK;
+}
+
+int check_flags(fs_solver* s) {
+    if (!s->cfg.check_finite) return FS_OK;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, s->flags, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (h) {
+        CK(cudaMemsetAsync(s->flags, 0, sizeof(int), s->stream));
+        s->stats.nonfinite = 1;
+        return fail(FS_ERR_NONFINITE, "the step produced a non-finite value");
+    }
+    return FS_OK;
+}
+
+int copy_in(fs_solver* s, float* dst, const float* host) {
+    CK(cudaMemcpy2DAsync(dst, s->pitch * sizeof(float), host, s->cols * sizeof(float), s->cols * sizeof(float),
+                         s->rows, cudaMemcpyHostToDevice, s->stream));
+    return FS_OK;
+}
+
+int copy_out(fs_solver* s, float* host, const float* src) {
+    CK(cudaMemcpy2DAsync(host, s->cols * sizeof(float), src, s->pitch * sizeof(float), s->cols * sizeof(float),
+                         s->rows, cudaMemcpyDeviceToHost, s->stream));
+    return FS_OK;
+}
+
+int copy_dd(fs_solver* s, float* dst, const float* src) {
+    if (dst == src) return FS_OK;
+    CK(cudaMemcpyAsync(dst, src, s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
+    return FS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fs_version(void) { return "fluid2d_gb300 " FS_VERSION " sm_103a"; }
+
+const char* fs_last_error(void) { return g_err.c_str(); }
+
+int fs_config_init(fs_config* cfg, int rows, int cols) {
+    if (!cfg) return fail(FS_ERR_ARG, "fs_config_init: null config");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->rows = rows;
+    cfg->cols = cols;
+    cfg->diffuse_iterations = 15;
+    cfg->pressure_iterations = 20;
+    cfg->smooth = 1;
+    cfg->sweeps_per_pass = 0;
+    cfg->tile_rows = 0;
+    cfg->use_graph = 1;
+    cfg->device = -1;
+    cfg->warm_start = FS_WARM_ZERO;
+    cfg->pressure_tolerance = 0.f;
+    cfg->pressure_max_iterations = 0;
+    cfg->check_finite = 1;
+    return FS_OK;
+}
+
+int fs_create(const fs_config* cfg, fs_solver** out) {
+    if (!cfg || !out) return fail(FS_ERR_ARG, "fs_create: null argument");
+    *out = nullptr;
+    if (cfg->rows < 3 || cfg->cols < 3) return fail(FS_ERR_ARG, "fs_create: rows and cols must be >= 3");
+    if ((long long)cfg->rows * cfg->cols > (1LL << 31)) return fail(FS_ERR_ARG, "fs_create: grid too large");
+    if (cfg->diffuse_iterations < 0 || cfg->pressure_iterations < 0)
+        return fail(FS_ERR_ARG, "fs_create: negative iteration count");
+    if (cfg->warm_start != FS_WARM_ZERO && cfg->warm_start != FS_WARM_PREVIOUS)
+        return fail(FS_ERR_ARG, "fs_create: unknown warm_start mode");
+    if (cfg->tile_rows != 0 && cfg->tile_rows != 64 && cfg->tile_rows != 128)
+        return fail(FS_ERR_ARG, "fs_create: tile_rows must be 0, 64 or 128");
+    if (cfg->pressure_tolerance > 0.f) return fail(FS_ERR_ARG, "fs_create: residual-driven pressure not enabled");
+
+    fs_solver* s = new fs_solver();
+    s->cfg = *cfg;
+    int dev = cfg->device;
+    if (dev < 0) {
+        if (cudaGetDevice(&dev) != cudaSuccess) {
+            delete s;
+            return fail(FS_ERR_CUDA, "fs_create: no CUDA device");
+        }
+    }
+    s->device = dev;
+    DeviceGuard g(dev);
+    s->rows = cfg->rows;
+    s->cols = cfg->cols;
+    s->pitch = (cfg->cols + 31) / 32 * 32;
+    s->field_floats = (size_t)s->rows * s->pitch;
+    s->tile_rows = cfg->tile_rows ? cfg->tile_rows : 64;
+    const int maxk = stencil_max_halo(s->tile_rows) - 1;
+    s->sweeps = cfg->sweeps_per_pass > 0 ? std::min(cfg->sweeps_per_pass, maxk) : std::min(8, maxk);
+
+    const int nfields = 6 + 9 + 6 + 2;
+    cudaError_t e = cudaMalloc(&s->slab, (size_t)nfields * s->field_floats * sizeof(float) + 256);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(e, "fs_create: cudaMalloc");
+    }
+    float* p = s->slab;
+    auto take = [&]() {
+        float* r = p;
+        p += s->field_floats;
+        return r;
+    };
+    for (int f = 0; f < 3; ++f) s->st[f] = take();
+    for (int f = 0; f < 3; ++f) s->src[f] = take();
+    for (int f = 0; f < 3; ++f) {
+        s->x0[f] = take();
+        s->pp[f][0] = take();
+        s->pp[f][1] = take();
+    }
+    s->acc = take();
+    s->div = take();
+    s->p[0] = take();
+    s->p[1] = take();
+    s->vel1[0] = take();
+    s->vel1[1] = take();
+    s->pwarm[0] = take();
+    s->pwarm[1] = take();
+    s->flags = reinterpret_cast<int*>(p);
+    int rc = FS_OK;
+    if ((e = cudaMemset(s->slab, 0, (size_t)nfields * s->field_floats * sizeof(float) + 256)) != cudaSuccess)
+        rc = cuda_fail(e, "fs_create: cudaMemset");
+    else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        rc = cuda_fail(e, "fs_create: cudaStreamCreate");
+    else if ((e = stencil_prepare()) != cudaSuccess)
+        rc = cuda_fail(e, "fs_create: stencil kernel attributes");
+    if (rc != FS_OK) {
+        if (s->stream) cudaStreamDestroy(s->stream);
+        cudaFree(s->slab);
+        delete s;
+        return rc;
+    }
+    s->stats.sweeps_per_pass = s->sweeps;
+    s->stats.tile_rows = s->tile_rows;
+    *out = s;
+    return FS_OK;
+}
+
+int fs_destroy(fs_solver* s) {
+    if (!s) return FS_OK;
+    DeviceGuard g(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    destroy_graph(s);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    cudaFree(s->slab);
+    delete s;
+    return FS_OK;
+}
+
+int fs_upload(fs_solver* s, const float* d, const float* u, const float* v) {
+    if (!s || !d || !u || !v) return fail(FS_ERR_ARG, "fs_upload: null argument");
+    DeviceGuard g(s->device);
+    int rc;
+    if ((rc = copy_in(s, s->st[F_D], d)) || (rc = copy_in(s, s->st[F_U], u)) || (rc = copy_in(s, s->st[F_V], v)))
+        return rc;
+    s->warm_valid = false;
+    return FS_OK;
+}
+
+int fs_upload_sources(fs_solver* s, const float* ds, const float* us, const float* vs) {
+    if (!s || !ds || !us || !vs) return fail(FS_ERR_ARG, "fs_upload_sources: null argument");
+    DeviceGuard g(s->device);
+    int rc;
+    if ((rc = copy_in(s, s->src[F_D], ds)) || (rc = copy_in(s, s->src[F_U], us)) ||
+        (rc = copy_in(s, s->src[F_V], vs)))
+        return rc;
+    return FS_OK;
+}
+
+int fs_download(fs_solver* s, float* d, float* u, float* v) {
+    if (!s || !d || !u || !v) return fail(FS_ERR_ARG, "fs_download: null argument");
+    DeviceGuard g(s->device);
+    int rc;
+    if ((rc = copy_out(s, d, s->st[F_D])) || (rc = copy_out(s, u, s->st[F_U])) || (rc = copy_out(s, v, s->st[F_V])))
+        return rc;
+    return FS_OK;
+}
+
+int fs_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, int nsteps) {
+    if (!s || nsteps < 0) return fail(FS_ERR_ARG, "fs_step: bad argument");
+    DeviceGuard g(s->device);
+    return run_steps(s, diffusion_rate, viscosity, dt, nsteps);
+}
+
+int fs_sync(fs_solver* s) {
+    if (!s) return fail(FS_ERR_ARG, "fs_sync: null handle");
+    DeviceGuard g(s->device);
+    CK(cudaStreamSynchronize(s->stream));
+    return check_flags(s);
+}
+
+int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate, float* u,
+                  float* v, const float* u_source, const float* v_source, float viscosity, float dt) {
+    if (!s || !density || !density_source || !u || !v || !u_source || !v_source)
+        return fail(FS_ERR_ARG, "fs_solve_host: null argument");
+    DeviceGuard g(s->device);
+    int rc;
+    if ((rc = copy_in(s, s->st[F_D], density)) || (rc = copy_in(s, s->st[F_U], u)) ||
+        (rc = copy_in(s, s->st[F_V], v)) || (rc = copy_in(s, s->src[F_D], density_source)) ||
+        (rc = copy_in(s, s->src[F_U], u_source)) || (rc = copy_in(s, s->src[F_V], v_source)))
+        return rc;
+    if ((rc = run_steps(s, diffusion_rate, viscosity, dt, 1)) != FS_OK) return rc;
+    if ((rc = copy_out(s, density, s->st[F_D])) || (rc = copy_out(s, u, s->st[F_U])) ||
+        (rc = copy_out(s, v, s->st[F_V])))
+        return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return check_flags(s);
+}
+
+int fs_stage(fs_solver* s, int stage, float rate, float dt) {
+    if (!s) return fail(FS_ERR_ARG, "fs_stage: null handle");
+    DeviceGuard g(s->device);
+    Counter cnt;
+    int rc = FS_OK;
+    switch (stage) {
+        case FS_STAGE_DIFFUSE_DENSITY: {
+            const int f[1] = {F_D};
+            const float r[1] = {rate};
+            float* out[1];
+            if ((rc = enqueue_diffuse(s, f, 1, r, dt, out, cnt)) == FS_OK) rc = copy_dd(s, s->st[F_D], out[0]);
+            break;
+        }
+        case FS_STAGE_DIFFUSE_VELOCITY: {
+            const int f[2] = {F_U, F_V};
+            const float r[2] = {rate, rate};
+            float* out[2];
+            if ((rc = enqueue_diffuse(s, f, 2, r, dt, out, cnt)) == FS_OK &&
+                (rc = copy_dd(s, s->st[F_U], out[0])) == FS_OK)
+                rc = copy_dd(s, s->st[F_V], out[1]);
+            break;
+        }
+        case FS_STAGE_ADVECT_DENSITY:
+            rc = enqueue_advect_density(s, s->st[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt);
+            break;
+        case FS_STAGE_PROJECT:
+            if ((rc = enqueue_project(s, s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], 0, cnt)) == FS_OK &&
+                (rc = copy_dd(s, s->st[F_U], s->vel1[0])) == FS_OK)
+                rc = copy_dd(s, s->st[F_V], s->vel1[1]);
+            break;
+        case FS_STAGE_ADVECT_VELOCITY: {
+            cudaError_t e = launch_advect_velocity(s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], advect_args(s, dt),
+                                                   s->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "advect_velocity");
+            cnt.launches++;
+            if ((rc = copy_dd(s, s->st[F_U], s->vel1[0])) == FS_OK) rc = copy_dd(s, s->st[F_V], s->vel1[1]);
+            break;
+        }
+        default:
+            return fail(FS_ERR_ARG, "fs_stage: unknown stage");
+    }
+    s->stats.kernel_launches += cnt.launches;
+    return rc;
+}
+
+int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, fs_kernel_times* out) {
+    if (!s || !out) return fail(FS_ERR_ARG, "fs_profile_step: null argument");
+    DeviceGuard g(s->device);
+    std::memset(out, 0, sizeof(*out));
+    s->prof = out;
+    s->prof_events.clear();
+    s->prof_marks.clear();
+    Counter cnt;
+    int rc = enqueue_step(s, diffusion_rate, viscosity, dt, cnt);
+    s->prof = nullptr;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (rc == FS_OK && e != cudaSuccess) rc = cuda_fail(e, "fs_profile_step: sync");
+    if (rc == FS_OK) {
+        for (size_t k = 0; k < s->prof_marks.size() && 2 * k + 1 < s->prof_events.size(); ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, s->prof_events[2 * k], s->prof_events[2 * k + 1]);
+            const int kind = s->prof_marks[k].first;
+            out->launches[kind] += 1;
+            out->ms[kind] += ms;
+            out->algorithmic_bytes[kind] += s->prof_marks[k].second;
+        }
+        s->stats.kernel_launches += cnt.launches;
+        s->stats.steps++;
+        s->warm_valid = true;
+    }
+    for (cudaEvent_t ev : s->prof_events) cudaEventDestroy(ev);
+    s->prof_events.clear();
+    s->prof_marks.clear();
+    return rc;
+}
+
+int fs_get_stats(const fs_solver* s, fs_stats* out) {
+    if (!s || !out) return fail(FS_ERR_ARG, "fs_get_stats: null argument");
+    *out = s->stats;
+    out->launches_per_step = s->launches_per_step;
+    out->passes_per_step = s->passes_per_step;
+    out->sweeps_per_pass = s->sweeps;
+    out->tile_rows = s->tile_rows;
+    out->pressure_iterations_last[0] = out->pressure_iterations_last[1] = s->cfg.pressure_iterations;
+    return FS_OK;
+}
+
+int fs_device_view_get(fs_solver* s, fs_device_view* out) {
+    if (!s || !out) return fail(FS_ERR_ARG, "fs_device_view_get: null argument");
+    out->density = s->st[F_D];
+    out->u = s->st[F_U];
+    out->v = s->st[F_V];
+    out->density_source = s->src[F_D];
+    out->u_source = s->src[F_U];
+    out->v_source = s->src[F_V];
+    out->rows = s->rows;
+    out->cols = s->cols;
+    out->pitch = s->pitch;
+    out->stream = (void*)s->stream;
+    return FS_OK;
+}
+
+int fs_host_alloc(void** ptr, unsigned long long bytes) {
+    if (!ptr) return fail(FS_ERR_ARG, "fs_host_alloc: null argument");
+    *ptr = nullptr;
+    cudaError_t e = cudaMallocHost(ptr, (size_t)bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost");
+    return FS_OK;
+}
+
+int fs_host_free(void* ptr) {
+    if (!ptr) return FS_OK;
+    CK(cudaFreeHost(ptr));
+    return FS_OK;
+}
+
+}  // extern "C"

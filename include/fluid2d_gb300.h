@@ -1,0 +1,168 @@
+/*
+ * fluid2d_gb300 — C ABI of a GB300-native (sm_103a) solver step for mworchel/fluid-2d.
+ *
+ * The reference exposes one operation, the abstract
+ *     fluid_solver::solve(density, density_src, diffusion_rate,
+ *                         u, v, u_src, v_src, viscosity, dt)
+ * (src/fluid_solver.hpp:16-24), implemented on the GPU by fluid_solver_gpu
+ * (src/fluid_solver_gpu.cuh:9-70, src/fluid_solver_gpu.cu:209-404). This header is the
+ * drop-in boundary for that operation: plain C, plain pointers and sizes, no C++ or
+ * torch types. A header-only adapter implementing the reference's class interface on top
+ * of it is in include/fluid_solver_gb300.hpp.
+ *
+ * Grids are row-major float32 arrays of rows*cols values, element (i, j) at i*cols + j,
+ * rows and cols INCLUDING the one-cell boundary — the layout of the reference's
+ * grid<float> (src/grid.hpp:60-69) and the (rows, cols) the reference's GPU solver is
+ * constructed with (src/fluid_solver_gpu.cuh:14, src/simulation.cpp:22).
+ *
+ * Every function returns an int status (FS_OK on success). The reference reports no
+ * errors at all (its solve() is void and ignores every cudaError_t); here a failed CUDA
+ * call, a bad argument, a non-finite result or an unconverged pressure solve each has a
+ * code, and fs_last_error() gives a message for the calling thread's last failure.
+ *
+ * Threading: a solver handle owns one CUDA stream on one device and is used by one host
+ * thread at a time. fs_solve_host() is synchronous like the reference; fs_step() and
+ * the upload/download calls are asynchronous on the handle's stream until fs_sync().
+ */
+#ifndef FLUID2D_GB300_H
+#define FLUID2D_GB300_H
+
+#if defined(__GNUC__)
+#define FS_API __attribute__((visibility("default")))
+#else
+#define FS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_OK 0
+#define FS_ERR_ARG 1          /* invalid argument (null pointer, size < 3, bad enum) */
+#define FS_ERR_CUDA 2         /* a CUDA runtime call failed; see fs_last_error() */
+#define FS_ERR_NONFINITE 3    /* the step produced a NaN or Inf (state is still updated) */
+#define FS_ERR_NOT_CONVERGED 4/* residual-driven pressure solve hit its iteration cap */
+#define FS_ERR_TIMEOUT 5      /* a bounded host wait ran out */
+#define FS_ERR_NOMEM 6        /* device or pinned host allocation failed */
+#define FS_ERR_STATE 7        /* call not valid in the handle's current state */
+
+/* Pressure warm start for the projection (the reference always starts from zero:
+ * p_buffer.clear(0), src/fluid_solver_gpu.cu:364). */
+#define FS_WARM_ZERO 0
+#define FS_WARM_PREVIOUS 1
+
+typedef struct fs_solver fs_solver;
+
+typedef struct fs_config {
+    int rows;                  /* grid rows including the boundary, >= 3 */
+    int cols;                  /* grid cols including the boundary, >= 3 */
+    int diffuse_iterations;    /* Jacobi sweeps per diffusion; reference: 15 (fluid_solver_gpu.cu:238) */
+    int pressure_iterations;   /* Jacobi sweeps per projection; reference: 20 (fluid_solver_gpu.cu:247) */
+    int smooth;                /* 1: 5-point density smoothing after advection (fluid_solver_gpu.cu:240) */
+    int sweeps_per_pass;       /* temporal-blocking depth (sweeps per HBM pass), 0 = tuned default */
+    int tile_rows;             /* stencil region height: 64 or 128, 0 = tuned default */
+    int use_graph;             /* 1: replay each step as a captured CUDA graph */
+    int device;                /* CUDA device ordinal, -1 = the calling thread's current device */
+    int warm_start;            /* FS_WARM_ZERO or FS_WARM_PREVIOUS */
+    float pressure_tolerance;  /* > 0: run the pressure solve to this relative residual */
+    int pressure_max_iterations; /* iteration cap when pressure_tolerance > 0 */
+    int check_finite;          /* 1: flag NaN/Inf in the step's outputs (FS_ERR_NONFINITE) */
+} fs_config;
+
+typedef struct fs_stats {
+    long long steps;                 /* solver steps completed */
+    long long kernel_launches;       /* kernels of this library launched so far */
+    int launches_per_step;           /* kernels per step in the current plan */
+    int passes_per_step;             /* HBM passes of the stencil kernels per step */
+    int sweeps_per_pass;             /* temporal-blocking depth in use */
+    int tile_rows;                   /* stencil region height in use */
+    int pressure_iterations_last[2]; /* sweeps used by the two projections of the last step */
+    double pressure_residual_last[2];/* their final relative residuals (residual mode only) */
+    int nonfinite;                   /* 1 if a NaN/Inf was flagged since the last check */
+} fs_stats;
+
+/* Device view of the resident state, for zero-copy use by other CUDA code. Each field
+ * is rows x pitch floats (pitch >= cols, a multiple of 32); element (i, j) at i*pitch + j. */
+typedef struct fs_device_view {
+    float* density;
+    float* u;
+    float* v;
+    float* density_source;
+    float* u_source;
+    float* v_source;
+    int rows, cols, pitch;
+    void* stream; /* cudaStream_t */
+} fs_device_view;
+
+/* Fill *cfg with the reference GPU solver's behaviour for a rows x cols grid:
+ * 15 diffusion sweeps, 20 pressure sweeps, smoothing on, zero warm start. */
+FS_API int fs_config_init(fs_config* cfg, int rows, int cols);
+
+/* Replaces fluid_solver_gpu::fluid_solver_gpu(rows, cols) (fluid_solver_gpu.cu:209-218):
+ * allocates the device state for one grid. */
+FS_API int fs_create(const fs_config* cfg, fs_solver** out);
+
+/* Replaces fluid_solver_gpu::~fluid_solver_gpu (fluid_solver_gpu.cu:220). NULL is a no-op. */
+FS_API int fs_destroy(fs_solver* s);
+
+/* Message for the calling thread's last failed call ("" when none). */
+FS_API const char* fs_last_error(void);
+
+/* Replaces fluid_solver_gpu::solve (fluid_solver_gpu.cu:222-258), argument for
+ * argument: uploads density/u/v and the three source grids from host memory, runs one
+ * step, downloads density/u/v, and returns when they are written. Host buffers may be
+ * pageable; pinned buffers (fs_host_alloc) copy faster. */
+FS_API int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate,
+                  float* u, float* v, const float* u_source, const float* v_source, float viscosity,
+                  float dt);
+
+/* Device-resident stepping (no per-step host round trip). */
+FS_API int fs_upload(fs_solver* s, const float* density, const float* u, const float* v);
+FS_API int fs_upload_sources(fs_solver* s, const float* density_source, const float* u_source,
+                      const float* v_source);
+FS_API int fs_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, int nsteps);
+FS_API int fs_download(fs_solver* s, float* density, float* u, float* v);
+FS_API int fs_sync(fs_solver* s);
+
+FS_API int fs_get_stats(const fs_solver* s, fs_stats* out);
+FS_API int fs_device_view_get(fs_solver* s, fs_device_view* out);
+
+/* Single stages of the step on the resident state, for kernel-level checks. The
+ * stage runs with the handle's sweep counts and leaves its result in the state. */
+#define FS_STAGE_DIFFUSE_DENSITY 1  /* add_sources + diffuse (fluid_solver_gpu.cu:237-238) */
+#define FS_STAGE_ADVECT_DENSITY 2   /* forward advection + smooth (fluid_solver_gpu.cu:239-240) */
+#define FS_STAGE_DIFFUSE_VELOCITY 3 /* add_sources + diffuse u, v (fluid_solver_gpu.cu:243-246) */
+#define FS_STAGE_PROJECT 4          /* project (fluid_solver_gpu.cu:358-404) */
+#define FS_STAGE_ADVECT_VELOCITY 5  /* backtrace advection of u, v (fluid_solver_gpu.cu:248-251) */
+FS_API int fs_stage(fs_solver* s, int stage, float rate, float dt);
+
+/* Per-kernel timing of one step. The step runs eagerly (not from the graph) with a
+ * CUDA event recorded on the handle's stream around every launch; for each kernel kind
+ * the result holds the launch count, the summed event time and the algorithmic bytes
+ * (each input field read once and each output written once per sweep, the cost model
+ * of the reference's one-kernel-per-sweep design). The state advances by one step. */
+#define FS_KIND_STENCIL 0   /* diffusion / pressure passes (temporally blocked) */
+#define FS_KIND_SPLAT 1     /* forward density advection */
+#define FS_KIND_FINISH 2    /* density fill + smoothing */
+#define FS_KIND_ADVECT 3    /* velocity backtrace advection */
+#define FS_KIND_MEMSET 4    /* accumulator clear (a memset node, not a kernel) */
+#define FS_NUM_KINDS 5
+typedef struct fs_kernel_times {
+    int launches[FS_NUM_KINDS];
+    double ms[FS_NUM_KINDS];
+    double algorithmic_bytes[FS_NUM_KINDS];
+} fs_kernel_times;
+FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, fs_kernel_times* out);
+
+/* Pinned host memory helpers (page-locked; fastest fs_solve_host / upload / download). */
+FS_API int fs_host_alloc(void** ptr, unsigned long long bytes);
+FS_API int fs_host_free(void* ptr);
+
+/* Library build identification: "fluid2d_gb300 <version> sm_103a". */
+FS_API const char* fs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUID2D_GB300_H */

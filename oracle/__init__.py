@@ -1,0 +1,174 @@
+"""ctypes wrappers for the oracle — TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline and
+reference legs import this package, and only to check or time against it. The
+product library (``fluid-2d_gb300``) never imports, links or calls anything here.
+
+Arrays are numpy, row-major ``[rows, cols]`` including the 1-cell boundary, the
+layout of the reference's ``grid<T>`` (src/grid.hpp:60-69). Every function works
+on copies and returns new arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import build_oracle as _b
+
+BND_CONT, BND_OPP_H, BND_OPP_V = 0, 1, 2
+
+_lib = None
+_ref = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_L, _I, _F = C.c_long, C.c_int, C.c_float
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _b.build_oracle()
+        L = C.CDLL(str(path))
+        L.orc_gpu_solve_f32.argtypes = [_L, _L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I, _I]
+        L.orc_gpu_solve_f64.argtypes = [_L, _L, _f64p, _f64p, _F, _f64p, _f64p, _f64p, _f64p, _F, _F, _I, _I, _I, _I]
+        L.orc_cpu_solve_f32.argtypes = [_L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I]
+        L.orc_add_sources_f32.argtypes = [_L, _L, _f32p, _f32p, _F]
+        L.orc_diffuse_f32.argtypes = [_L, _L, _f32p, _I, _F, _F, _I]
+        L.orc_set_bnd_f32.argtypes = [_L, _L, _f32p, _I]
+        L.orc_advect_trace_f32.argtypes = [_L, _L, _f32p, _f32p, _f32p, _F]
+        L.orc_smooth_f32.argtypes = [_L, _L, _f32p]
+        L.orc_advect_velocity_f32.argtypes = [_L, _L, _f32p, _f32p, _F]
+        L.orc_project_f32.argtypes = [_L, _L, _f32p, _f32p, _I, C.c_void_p, C.c_void_p]
+        L.orc_project_f64.argtypes = [_L, _L, _f64p, _f64p, _I, C.c_void_p, C.c_void_p]
+        L.orc_residual_f32.argtypes = [_L, _L, _f32p, _f32p]
+        L.orc_residual_f32.restype = C.c_double
+        L.orc_residual_f64.argtypes = [_L, _L, _f64p, _f64p]
+        L.orc_residual_f64.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The compiled reference host solver, or None where the reference checkout is absent."""
+    global _ref
+    if _ref is None:
+        path = _b.REF_OUT / "libref_cpu.so"
+        if not path.exists():
+            built = _b.build_ref()
+            if built is None:
+                return None
+            path = built
+        R = C.CDLL(str(path))
+        R.ref_cpu_solve.argtypes = [_L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I]
+        _ref = R
+    return _ref
+
+
+def _c(a, dt=np.float32):
+    return np.ascontiguousarray(a, dtype=dt).copy()
+
+
+def _chk(rc):
+    if rc != 0:
+        raise ValueError("oracle rejected its arguments")
+
+
+# ---------------------------------------------------------------- whole steps
+
+def gpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=15, kp=20, smooth=True, nsteps=1, f64=False):
+    """fluid_solver_gpu::solve semantics (fluid_solver_gpu.cu:222-258), nsteps times."""
+    t = np.float64 if f64 else np.float32
+    d, ds, u, v, us, vs = (_c(a, t) for a in (d, ds, u, v, us, vs))
+    fn = lib().orc_gpu_solve_f64 if f64 else lib().orc_gpu_solve_f32
+    _chk(fn(d.shape[0], d.shape[1], d, ds, diff, u, v, us, vs, visc, dt, kd, kp, int(smooth), nsteps))
+    return d, u, v
+
+
+def cpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=20, kp=20, nsteps=1):
+    """fluid_solver_cpu::solve semantics (fluid_solver_cpu.cpp:6-31), nsteps times."""
+    d, ds, u, v, us, vs = (_c(a) for a in (d, ds, u, v, us, vs))
+    _chk(lib().orc_cpu_solve_f32(d.shape[0], d, ds, diff, u, v, us, vs, visc, dt, kd, kp, nsteps))
+    return d, u, v
+
+
+def ref_cpu_solve(d, ds, diff, u, v, us, vs, visc, dt, nsteps=1):
+    """The compiled reference host solver itself (20/20 Gauss-Seidel sweeps)."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("reference sources not present; compiled reference unavailable")
+    d, ds, u, v, us, vs = (_c(a) for a in (d, ds, u, v, us, vs))
+    _chk(R.ref_cpu_solve(d.shape[0], d, ds, diff, u, v, us, vs, visc, dt, nsteps))
+    return d, u, v
+
+
+# ---------------------------------------------------------------- single stages
+
+def add_sources(x, s, dt):
+    x, s = _c(x), _c(s)
+    _chk(lib().orc_add_sources_f32(x.shape[0], x.shape[1], x, s, dt))
+    return x
+
+
+def set_bnd(x, mode):
+    x = _c(x)
+    _chk(lib().orc_set_bnd_f32(x.shape[0], x.shape[1], x, mode))
+    return x
+
+
+def diffuse(x, mode, rate, dt, iters):
+    x = _c(x)
+    _chk(lib().orc_diffuse_f32(x.shape[0], x.shape[1], x, mode, rate, dt, iters))
+    return x
+
+
+def advect_trace(d, u, v, dt):
+    d, u, v = _c(d), _c(u), _c(v)
+    _chk(lib().orc_advect_trace_f32(d.shape[0], d.shape[1], d, u, v, dt))
+    return d
+
+
+def smooth(d):
+    d = _c(d)
+    _chk(lib().orc_smooth_f32(d.shape[0], d.shape[1], d))
+    return d
+
+
+def advect_velocity(u, v, dt):
+    u, v = _c(u), _c(v)
+    _chk(lib().orc_advect_velocity_f32(u.shape[0], u.shape[1], u, v, dt))
+    return u, v
+
+
+def project(u, v, iters, p0=None, f64=False):
+    """Returns (u, v, p, div). p0 is the starting pressure (zero when None)."""
+    t = np.float64 if f64 else np.float32
+    u, v = _c(u, t), _c(v, t)
+    p = _c(p0, t) if p0 is not None else np.zeros_like(u)
+    dv = np.zeros_like(u)
+    fn = lib().orc_project_f64 if f64 else lib().orc_project_f32
+    _chk(fn(u.shape[0], u.shape[1], u, v, iters, p.ctypes.data, dv.ctypes.data))
+    return u, v, p, dv
+
+
+def residual(p, div):
+    """Relative Poisson residual ||div + sum(nbrs) - 4p|| / ||div|| over the interior."""
+    if p.dtype == np.float64:
+        return lib().orc_residual_f64(p.shape[0], p.shape[1], _c(p, np.float64), _c(div, np.float64))
+    return lib().orc_residual_f32(p.shape[0], p.shape[1], _c(p), _c(div))
+
+
+def rel_linf(x, y, skip_corners=True):
+    """max|x - y| / max|y| over all cells, the four corners excluded by default."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    m = np.ones(x.shape, bool)
+    if skip_corners:
+        m[0, 0] = m[0, -1] = m[-1, 0] = m[-1, -1] = False
+    den = np.max(np.abs(y[m])) if m.any() else 0.0
+    num = np.max(np.abs(x[m] - y[m])) if m.any() else 0.0
+    if den == 0.0:
+        return float(num)
+    return float(num / den)

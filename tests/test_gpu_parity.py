@@ -1,0 +1,218 @@
+"""CUDA path vs the oracle's restatement of fluid_solver_gpu.cu (GPU required).
+
+Tolerance: relative L-infinity, max|gpu - oracle| / max|oracle| over every cell but the
+four corners, <= 1e-5 per field per step (the bar the solver is built to). Stages
+whose arithmetic has no atomics are also checked at 1e-6 or bit-exactly; the density
+splat adds with fp32 atomics in an unspecified order, as the reference does.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+SIZES = [(3, 3), (4, 5), (5, 5), (9, 7), (33, 33), (34, 34), (35, 61), (66, 66), (111, 130), (130, 130),
+         (131, 131)]
+
+
+def make_solver(fluid, rows, cols, **kw):
+    kw.setdefault("device", 0)
+    return fluid.Solver(rows, cols, **kw)
+
+
+def rand(wl, rows, cols, seed, vmax=0.02):
+    return wl.random_state(rows, cols, seed, vmax=vmax)
+
+
+@pytest.mark.parametrize("rows,cols", SIZES)
+@pytest.mark.parametrize("sweeps,tile_rows", [(1, 64), (3, 64), (8, 64), (8, 128), (13, 128)])
+def test_diffuse_density_stage(fluid, wl, rows, cols, sweeps, tile_rows):
+    d, u, v, ds, us, vs = rand(wl, rows, cols, rows * 31 + cols)
+    kd, rate, dt = 17, 3e-3, 0.1
+    with make_solver(fluid, rows, cols, diffuse_iterations=kd, sweeps_per_pass=sweeps, tile_rows=tile_rows) as s:
+        s.upload(d, u, v)
+        s.upload_sources(ds, us, vs)
+        s.stage(fluid.STAGE_DIFFUSE_DENSITY, rate, dt)
+        gd, gu, gv = s.download()
+    want = oracle.diffuse(oracle.add_sources(d, ds, dt), oracle.BND_CONT, rate, dt, kd)
+    assert oracle.rel_linf(gd, want) <= 1e-6
+    np.testing.assert_array_equal(gu, u)  # untouched
+
+
+@pytest.mark.parametrize("rows,cols", [(5, 5), (34, 34), (35, 61), (130, 130)])
+@pytest.mark.parametrize("kd", [0, 1, 15, 40])
+def test_diffuse_velocity_stage(fluid, wl, rows, cols, kd):
+    d, u, v, ds, us, vs = rand(wl, rows, cols, 7 + kd)
+    rate, dt = 1e-2, 0.1
+    with make_solver(fluid, rows, cols, diffuse_iterations=kd) as s:
+        s.upload(d, u, v)
+        s.upload_sources(ds, us, vs)
+        s.stage(fluid.STAGE_DIFFUSE_VELOCITY, rate, dt)
+        _, gu, gv = s.download()
+    wu = oracle.diffuse(oracle.add_sources(u, us, dt), oracle.BND_OPP_H, rate, dt, kd)
+    wv = oracle.diffuse(oracle.add_sources(v, vs, dt), oracle.BND_OPP_V, rate, dt, kd)
+    assert oracle.rel_linf(gu, wu) <= 1e-6
+    assert oracle.rel_linf(gv, wv) <= 1e-6
+    # corners are never written
+    for g, x in ((gu, u), (gv, v)):
+        assert g[0, 0] == x[0, 0] and g[-1, -1] == x[-1, -1]
+
+
+@pytest.mark.parametrize("rows,cols", SIZES)
+@pytest.mark.parametrize("kp,sweeps,tile_rows", [(20, 8, 64), (20, 1, 64), (0, 8, 64), (40, 8, 128), (7, 3, 128)])
+def test_project_stage(fluid, wl, rows, cols, kp, sweeps, tile_rows):
+    d, u, v, ds, us, vs = rand(wl, rows, cols, rows + 3 * cols, vmax=1.0)
+    with make_solver(fluid, rows, cols, pressure_iterations=kp, sweeps_per_pass=sweeps, tile_rows=tile_rows) as s:
+        s.upload(d, u, v)
+        s.stage(fluid.STAGE_PROJECT, 0.0, 0.1)
+        _, gu, gv = s.download()
+    wu, wv, _, _ = oracle.project(u, v, kp)
+    assert oracle.rel_linf(gu, wu) <= 1e-6
+    assert oracle.rel_linf(gv, wv) <= 1e-6
+
+
+@pytest.mark.parametrize("rows,cols", SIZES)
+def test_advect_velocity_stage_bit_exact(fluid, wl, rows, cols):
+    d, u, v, ds, us, vs = rand(wl, rows, cols, 99 + rows, vmax=0.05)
+    dt = 0.1
+    with make_solver(fluid, rows, cols) as s:
+        s.upload(d, u, v)
+        s.stage(fluid.STAGE_ADVECT_VELOCITY, 0.0, dt)
+        _, gu, gv = s.download()
+    wu, wv = oracle.advect_velocity(u, v, dt)
+    np.testing.assert_array_equal(gu, wu)
+    np.testing.assert_array_equal(gv, wv)
+
+
+@pytest.mark.parametrize("rows,cols", SIZES)
+@pytest.mark.parametrize("smooth", [1, 0])
+def test_advect_density_stage(fluid, wl, rows, cols, smooth):
+    d, u, v, ds, us, vs = rand(wl, rows, cols, 5 + rows, vmax=0.05)
+    dt = 0.1
+    with make_solver(fluid, rows, cols, smooth=smooth) as s:
+        s.upload(d, u, v)
+        s.stage(fluid.STAGE_ADVECT_DENSITY, 0.0, dt)
+        gd, _, _ = s.download()
+    want = oracle.advect_trace(d, u, v, dt)
+    if smooth:
+        want = oracle.smooth(want)
+    assert oracle.rel_linf(gd, want, skip_corners=False) <= 1e-6
+
+
+def _run_lockstep(fluid, w, steps, kd, kp, **cfg):
+    """Run the GPU and the oracle side by side from the same state; return the worst
+    per-step relative error of each field."""
+    d, u, v = w.state()
+    od, ou, ov = w.state()
+    worst = [0.0, 0.0, 0.0]
+    with make_solver(fluid, w.rows, w.cols, diffuse_iterations=kd, pressure_iterations=kp, **cfg) as s:
+        for _ in range(steps):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            od, ou, ov = oracle.gpu_solve(od, w.ds, w.diffusion, ou, ov, w.us, w.vs, w.viscosity, w.dt, kd=kd, kp=kp)
+            for k, (g, o) in enumerate(((d, od), (u, ou), (v, ov))):
+                worst[k] = max(worst[k], oracle.rel_linf(g, o))
+        st = s.stats()
+    return worst, st
+
+
+def test_small_sources_100_steps(fluid, wl):
+    """N=128 (130x130), dt 0.1, rates 1e-4, 20/20 sweeps, 100 steps."""
+    w = wl.small_sources(128, seed=1)
+    worst, st = _run_lockstep(fluid, w, 100, 20, 20)
+    assert max(worst) <= TOL, worst
+    assert st["steps"] == 100 and st["kernel_launches"] >= 100 * st["launches_per_step"]
+
+
+@pytest.mark.parametrize("n,seed", [(32, 3), (61, 4), (127, 5)])
+def test_reference_counts_steps(fluid, wl, n, seed):
+    """The reference's own 15/20 sweeps and default constructor."""
+    w = wl.small_sources(n, seed=seed)
+    worst, _ = _run_lockstep(fluid, w, 20, 15, 20)
+    assert max(worst) <= TOL, worst
+
+
+def test_vortex_field_steps(fluid, wl):
+    w = wl.vortex_field(256, seed=2, kd=40, kp=40, vortices=8, rmin=8, rmax=30)
+    worst, _ = _run_lockstep(fluid, w, 10, 40, 40)
+    assert max(worst) <= TOL, worst
+
+
+def test_non_square(fluid, wl):
+    rows, cols = 47, 90
+    d, u, v, ds, us, vs = rand(wl, rows, cols, 12, vmax=0.02)
+    w = wl.Workload("ns", rows, cols, 0.1, 1e-3, 1e-3, 15, 20, d, u, v, ds, us, vs)
+    worst, _ = _run_lockstep(fluid, w, 10, 15, 20)
+    assert max(worst) <= TOL, worst
+
+
+@pytest.mark.parametrize("sweeps,tile_rows", [(1, 64), (2, 64), (5, 128), (8, 128), (20, 128)])
+def test_blocking_depth_does_not_change_results(fluid, wl, sweeps, tile_rows):
+    w = wl.small_sources(96, seed=8)
+    worst, st = _run_lockstep(fluid, w, 5, 20, 20, sweeps_per_pass=sweeps, tile_rows=tile_rows)
+    assert max(worst) <= TOL, worst
+
+
+def test_graph_replay_equals_eager(fluid, wl):
+    w = wl.small_sources(64, seed=9)
+    outs = []
+    for use_graph in (0, 1):
+        with make_solver(fluid, w.rows, w.cols, use_graph=use_graph) as s:
+            s.upload(*w.state())
+            s.upload_sources(*w.sources())
+            s.step(w.diffusion, w.viscosity, w.dt, nsteps=10)
+            outs.append(s.download())
+    for a, b in zip(*outs):
+        assert oracle.rel_linf(a, b) <= 1e-6
+
+
+def test_device_resident_equals_solve_host(fluid, wl):
+    w = wl.small_sources(48, seed=10)
+    d, u, v = w.state()
+    with make_solver(fluid, w.rows, w.cols) as s:
+        for _ in range(5):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+    with make_solver(fluid, w.rows, w.cols) as s:
+        s.upload(*w.state())
+        s.upload_sources(*w.sources())
+        s.step(w.diffusion, w.viscosity, w.dt, nsteps=5)
+        rd, ru, rv = s.download()
+    for a, b in ((d, rd), (u, ru), (v, rv)):
+        assert oracle.rel_linf(a, b) <= 1e-6
+
+
+def test_zero_stays_zero_and_rest_is_steady(fluid):
+    n = 40
+    z = np.zeros((n, n), np.float32)
+    with make_solver(fluid, n, n) as s:
+        d, u, v = z.copy(), z.copy(), z.copy()
+        s.solve(d, z, 1e-3, u, v, z, z, 1e-3, 0.1)
+        assert not d.any() and not u.any() and not v.any()
+        d = np.ones((n, n), np.float32)
+        s.solve(d, z, 1e-2, u, v, z, z, 1e-2, 0.1)
+        np.testing.assert_array_equal(d[1:-1, 1:-1], 1.0)
+
+
+def test_nonfinite_is_reported(fluid, wl):
+    n = 20
+    d, u, v, ds, us, vs = rand(wl, n, n, 3)
+    d[5, 5] = np.nan
+    with make_solver(fluid, n, n) as s:
+        with pytest.raises(fluid.FluidError) as e:
+            s.solve(d, ds, 1e-3, u, v, us, vs, 1e-3, 0.1)
+        assert e.value.code == fluid.FS_ERR_NONFINITE
+        # the handle stays usable
+        d2, u2, v2, ds2, us2, vs2 = rand(wl, n, n, 4)
+        s.solve(d2, ds2, 1e-3, u2, v2, us2, vs2, 1e-3, 0.1)
+        assert np.isfinite(d2).all()
+
+
+def test_shape_and_dtype_checks(fluid):
+    with make_solver(fluid, 10, 10) as s:
+        bad = np.zeros((10, 11), np.float32)
+        ok = np.zeros((10, 10), np.float32)
+        with pytest.raises(ValueError):
+            s.solve(bad, ok, 0.0, ok, ok, ok, ok, 0.0, 0.1)
+        with pytest.raises(TypeError):
+            s.solve(ok.astype(np.float64), ok, 0.0, ok, ok, ok, ok, 0.0, 0.1)

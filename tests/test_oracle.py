@@ -1,0 +1,127 @@
+"""The oracle against the reference: golden fixtures from the compiled reference host
+solver, the oracle's own fixtures, and known answers of the method (CPU only)."""
+import pathlib
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+CASES = sorted(p.name[len("ref_cpu_"):-4] for p in GOLDEN.glob("ref_cpu_*.npz"))
+
+
+def _inputs(z):
+    diff, visc, dt = (float(x) for x in z["params"])
+    return (z["d"], z["ds"], diff, z["u"], z["v"], z["us"], z["vs"], visc, dt), int(z["steps"])
+
+
+def test_fixtures_present():
+    assert len(CASES) >= 5
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cpu_semantics_bit_exact_vs_reference_fixture(case):
+    """fluid_solver_cpu.cpp:6-215 restated == the compiled reference, bit for bit."""
+    z = np.load(GOLDEN / f"ref_cpu_{case}.npz")
+    args, steps = _inputs(z)
+    d, u, v = oracle.cpu_solve(*args, kd=20, kp=20, nsteps=steps)
+    for got, key in ((d, "out_d"), (u, "out_u"), (v, "out_v")):
+        np.testing.assert_array_equal(got, z[key])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_semantics_reproduces_its_fixture(case):
+    """fluid_solver_gpu.cu semantics: the oracle rebuilt here gives the committed bits."""
+    z = np.load(GOLDEN / f"oracle_gpu_{case}.npz")
+    args, steps = _inputs(z)
+    kd, kp = (int(x) for x in z["iters"])
+    d, u, v = oracle.gpu_solve(*args, kd=kd, kp=kp, nsteps=steps)
+    for got, key in ((d, "out_d"), (u, "out_u"), (v, "out_v")):
+        np.testing.assert_array_equal(got, z[key])
+
+
+def test_live_reference_vs_port(wl):
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources not present on this machine")
+    for n, seed in ((4, 1), (9, 2), (17, 3), (40, 4)):
+        d, u, v, ds, us, vs = wl.random_state(n, n, seed, vmax=0.2)
+        args = (d, ds, 0.05, u, v, us, vs, 0.02, 0.1)
+        r = oracle.ref_cpu_solve(*args, nsteps=3)
+        p = oracle.cpu_solve(*args, nsteps=3)
+        for a, b in zip(r, p):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_gpu_and_cpu_semantics_differ(wl):
+    """The reference's two solvers are different methods (Jacobi vs Gauss-Seidel,
+    smoothing, corner handling); parity must name which one it targets."""
+    w = wl.small_sources(32, seed=3)
+    args = (w.d, w.ds, w.diffusion, w.u, w.v, w.us, w.vs, w.viscosity, w.dt)
+    g = oracle.gpu_solve(*args, kd=20, kp=20, nsteps=5)
+    c = oracle.cpu_solve(*args, kd=20, kp=20, nsteps=5)
+    assert oracle.rel_linf(g[0], c[0]) > 1e-3
+
+
+# ------------------------------------------------------------------ known answers
+
+def test_zero_state_stays_zero():
+    z = np.zeros((20, 17), np.float32)
+    d, u, v = oracle.gpu_solve(z, z, 1e-3, z, z, z, z, 1e-3, 0.1, nsteps=3)
+    assert not d.any() and not u.any() and not v.any()
+
+
+def test_uniform_density_at_rest_is_steady():
+    n = 24
+    d = np.ones((n, n), np.float32)
+    z = np.zeros_like(d)
+    out, u, v = oracle.gpu_solve(d, z, 1e-2, z, z, z, z, 1e-2, 0.1, nsteps=2)
+    np.testing.assert_array_equal(out[1:-1, 1:-1], 1.0)
+    np.testing.assert_array_equal(out[0, 1:-1], 1.0)
+
+
+def test_diffusion_of_uniform_field_is_identity():
+    x = np.full((15, 15), 3.0, np.float32)
+    y = oracle.diffuse(x, oracle.BND_CONT, 0.7, 0.1, 9)
+    np.testing.assert_allclose(y[1:-1, 1:-1], 3.0, rtol=1e-6)
+
+
+def test_trace_advection_conserves_mass_away_from_walls():
+    n = 64
+    d = np.zeros((n, n), np.float32)
+    d[28:36, 28:36] = 1.0
+    u = np.full_like(d, 0.013)
+    v = np.full_like(d, -0.021)
+    out = oracle.advect_trace(d, u, v, 0.05)
+    assert abs(float(out.sum(dtype=np.float64)) - 64.0) < 1e-4
+
+
+def test_projection_subtracts_the_solved_pressure_gradient(wl):
+    """u1 = u - 0.5 (p[j+1] - p[j-1]) / h on the interior (remove_p_kernel)."""
+    n = 18
+    _, u, v, _, _, _ = wl.random_state(n, n, 5)
+    u1, v1, p, _ = oracle.project(u, v, 50)
+    h = np.float32(1.0) / np.sqrt(np.float32(n * n))
+    gu = (np.float32(0.5) * (p[1:-1, 2:] - p[1:-1, :-2])) / h
+    gv = (np.float32(0.5) * (p[2:, 1:-1] - p[:-2, 1:-1])) / h
+    np.testing.assert_array_equal(u1[1:-1, 1:-1], u[1:-1, 1:-1] - gu)
+    np.testing.assert_array_equal(v1[1:-1, 1:-1], v[1:-1, 1:-1] - gv)
+    np.testing.assert_array_equal(u1[1:-1, 0], -u1[1:-1, 1])
+    np.testing.assert_array_equal(v1[0, 1:-1], -v1[1, 1:-1])
+
+
+def test_jacobi_residual_decreases(wl):
+    n = 34
+    _, u, v, _, _, _ = wl.random_state(n, n, 6)
+    _, _, p10, dv = oracle.project(u, v, 10)
+    _, _, p200, _ = oracle.project(u, v, 200)
+    assert oracle.residual(p200, dv) < oracle.residual(p10, dv) < 1.0
+
+
+def test_fp64_rerun_tracks_fp32(wl):
+    w = wl.small_sources(32, seed=4)
+    args = (w.d, w.ds, w.diffusion, w.u, w.v, w.us, w.vs, w.viscosity, w.dt)
+    f = oracle.gpu_solve(*args, nsteps=10)
+    g = oracle.gpu_solve(*args, nsteps=10, f64=True)
+    for a, b in zip(f, g):
+        assert oracle.rel_linf(a, b) < 1e-3
