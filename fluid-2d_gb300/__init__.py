@@ -84,6 +84,7 @@ SIGNATURES = {
     "fs_device_view_get": (C.c_int, [_P, C.POINTER(fs_device_view)]),
     "fs_stage": (C.c_int, [_P, _I, _F, _F]),
     "fs_profile_step": (C.c_int, [_P, _F, _F, _F, C.POINTER(fs_kernel_times)]),
+    "fs_project_noalloc": (C.c_int, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
     "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
     "fs_host_free": (C.c_int, [_P]),
     "fs_version": (C.c_char_p, []),

@@ -82,6 +82,9 @@ inline void tile_split(int n, int tile, int* count, int* shift) {
     *count = (n + s + tile - 1) / tile;
 }
 
+// Sets the calling thread's fs_last_error() message and returns code (solver.cu).
+int record_error(int code, const char* msg);
+
 // Launchers (stencil.cu, advect.cu).
 cudaError_t stencil_prepare();
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st);

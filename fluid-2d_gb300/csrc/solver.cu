@@ -72,6 +72,9 @@ enum FieldId { F_D = 0, F_U = 1, F_V = 2 };
 
 }  // namespace
 
+// Lets other translation units of the library report through fs_last_error().
+int fs::record_error(int code, const char* msg) { return fail(code, msg); }
+
 struct fs_solver {
     fs_config cfg{};
     int device = 0;

@@ -154,6 +154,29 @@ typedef struct fs_kernel_times {
 } fs_kernel_times;
 FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, fs_kernel_times* out);
 
+/* Pressure projection that allocates nothing. No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: code running inside a host framework that
+ * owns all device memory, code issuing work while a stream capture is recorded
+ * (cudaMalloc is not allowed inside a global-mode capture), and frame loops that must
+ * not allocate after start-up. fs_create() allocates, so they cannot use a handle.
+ *
+ * Projects (u, v) -> (u_out, v_out) with `iterations` Jacobi sweeps from zero pressure,
+ * exactly as a handle's projection stage (fluid_solver_gpu.cu:358-404 semantics). All
+ * four arrays are the caller's device buffers of rows x pitch floats (element (i, j) at
+ * i*pitch + j, rows/cols including the boundary); outputs must not alias inputs. Work is
+ * queued on `stream` (a cudaStream_t; NULL = default stream) and is asynchronous.
+ *
+ * Scratch (divergence and two pressure buffers) lives in a fixed file-scope device
+ * array of 3 x FS_NOALLOC_MAX_CELLS floats (12 MiB) that every GPU loading this library
+ * holds until process exit; rows * pitch above FS_NOALLOC_MAX_CELLS is rejected with
+ * FS_ERR_ARG. The first call on a device looks up that array's address and caches it:
+ * make it before any stream capture. All calls share the array, so calls that may
+ * overlap on the GPU race and must be serialised by the caller. */
+#define FS_NOALLOC_MAX_CELLS 1048576
+FS_API int fs_project_noalloc(const float* u, const float* v, float* u_out, float* v_out, int rows, int cols,
+                              int pitch, int iterations, void* stream);
+
 /* Pinned host memory helpers (page-locked; fastest fs_solve_host / upload / download). */
 FS_API int fs_host_alloc(void** ptr, unsigned long long bytes);
 FS_API int fs_host_free(void* ptr);
