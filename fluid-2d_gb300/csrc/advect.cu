@@ -16,33 +16,33 @@
 // intrinsics keep the compiler from contracting them into FMAs. The splat order of
 // the atomics is unspecified, as in the reference.
 
+#include <algorithm>
+
 #include "fs_internal.cuh"
 
 namespace fs {
 namespace {
 
-__global__ void __launch_bounds__(256) splat_kernel(const float* __restrict__ d0, const float* __restrict__ u,
-                                                    const float* __restrict__ v, float* __restrict__ acc,
-                                                    const AdvectArgs A) {
+// Forward splat of interior source cell (i, j), advect_trace_kernel
+// (fluid_solver_gpu.cu:141-159).
+__device__ __forceinline__ void splat_cell(const float* __restrict__ d0, const float* __restrict__ u,
+                                           const float* __restrict__ v, float* __restrict__ acc, const AdvectArgs& A,
+                                           int i, int j) {
     const size_t P = (size_t)A.pitch;
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y + 1; i < A.rows - 1; i += blockDim.y * gridDim.y) {
-        for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j < A.cols - 1; j += blockDim.x * gridDim.x) {
-            const size_t o = (size_t)i * P + j;
-            const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, __ldg(u + o)));
-            const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, __ldg(v + o)));
-            // skipped unless inside [0.5, n-1.5] (fluid_solver_gpu.cu:144); NaN is skipped too
-            if (!(x >= 0.5f && x <= A.xmax && y >= 0.5f && y <= A.ymax)) continue;
-            const int j0 = (int)x, i0 = (int)y;
-            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
-            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
-            const float d = __ldg(d0 + o);
-            float* t = acc + (size_t)i0 * P + j0;
-            atomicAdd(t, __fmul_rn(__fmul_rn(s1, s3), d));
-            atomicAdd(t + P, __fmul_rn(__fmul_rn(s1, s2), d));
-            atomicAdd(t + 1, __fmul_rn(__fmul_rn(s0, s3), d));
-            atomicAdd(t + P + 1, __fmul_rn(__fmul_rn(s0, s2), d));
-        }
-    }
+    const size_t o = (size_t)i * P + j;
+    const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, __ldg(u + o)));
+    const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, __ldg(v + o)));
+    // skipped unless inside [0.5, n-1.5] (fluid_solver_gpu.cu:144); NaN is skipped too
+    if (!(x >= 0.5f && x <= A.xmax && y >= 0.5f && y <= A.ymax)) return;
+    const int j0 = (int)x, i0 = (int)y;
+    const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+    const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+    const float d = __ldg(d0 + o);
+    float* t = acc + (size_t)i0 * P + j0;
+    atomicAdd(t, __fmul_rn(__fmul_rn(s1, s3), d));
+    atomicAdd(t + P, __fmul_rn(__fmul_rn(s1, s2), d));
+    atomicAdd(t + 1, __fmul_rn(__fmul_rn(s0, s3), d));
+    atomicAdd(t + P + 1, __fmul_rn(__fmul_rn(s0, s2), d));
 }
 
 // Value of the accumulator after set_boundary_continuous (fluid_solver_gpu.cu:11-24):
@@ -54,71 +54,127 @@ __device__ __forceinline__ float filled(const float* __restrict__ acc, int r, in
     return __ldg(acc + (size_t)r * A.pitch + c);
 }
 
+// Neumann fill of the splat result plus smooth_kernel (fluid_solver_gpu.cu:94) for
+// cell (i, j); returns 1 if the value is not finite.
+__device__ __forceinline__ int finish_cell(const float* __restrict__ acc, float* __restrict__ d, int smooth,
+                                           const AdvectArgs& A, int i, int j) {
+    float out = filled(acc, i, j, A);
+    if (smooth && i >= 1 && i <= A.rows - 2 && j >= 1 && j <= A.cols - 2) {
+        // 0.2f * (c + l + r + u + d)
+        float s = __fadd_rn(out, filled(acc, i, j - 1, A));
+        s = __fadd_rn(s, filled(acc, i, j + 1, A));
+        s = __fadd_rn(s, filled(acc, i - 1, j, A));
+        s = __fadd_rn(s, filled(acc, i + 1, j, A));
+        out = __fmul_rn(0.2f, s);
+    }
+    d[(size_t)i * A.pitch + j] = out;
+    return !isfinite(out);
+}
+
+// Backtrace advection of u and v for cell (i, j), advect_kernel
+// (fluid_solver_gpu.cu:111-126), with the reflecting fills for edge cells.
+__device__ __forceinline__ void advect_cell(const float* __restrict__ u0, const float* __restrict__ v0,
+                                            float* __restrict__ u, float* __restrict__ v, const AdvectArgs& A, int i,
+                                            int j) {
+    const size_t P = (size_t)A.pitch;
+    const bool ri = i >= 1 && i <= A.rows - 2, ci = j >= 1 && j <= A.cols - 2;
+    const size_t o = (size_t)i * P + j;
+    if (!ri && !ci) {  // corners are never written by the reference
+        u[o] = __ldg(u0 + o);
+        v[o] = __ldg(v0 + o);
+        return;
+    }
+    // Edge cells copy the advected inner neighbour: u is negated on the left/right
+    // edges, v on the top/bottom edges (fluid_solver_gpu.cu:26-54).
+    int si = i, sj = j;
+    float su = 1.f, sv = 1.f;
+    if (!ci) {
+        sj = (j == 0) ? 1 : A.cols - 2;
+        su = -1.f;
+    } else if (!ri) {
+        si = (i == 0) ? 1 : A.rows - 2;
+        sv = -1.f;
+    }
+    const size_t so = (size_t)si * P + sj;
+    float x = __fsub_rn((float)sj, __fmul_rn(A.dt0, __ldg(u0 + so)));
+    float y = __fsub_rn((float)si, __fmul_rn(A.dt0, __ldg(v0 + so)));
+    x = fmaxf(1.5f, fminf(A.xmax, x));
+    y = fmaxf(1.5f, fminf(A.ymax, y));
+    const int j0 = (int)x, i0 = (int)y;
+    const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+    const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+    const size_t q = (size_t)i0 * P + j0;
+    const float ua = __ldg(u0 + q), ub = __ldg(u0 + q + 1), uc = __ldg(u0 + q + P), ud = __ldg(u0 + q + P + 1);
+    const float va = __ldg(v0 + q), vb = __ldg(v0 + q + 1), vc = __ldg(v0 + q + P), vd = __ldg(v0 + q + P + 1);
+    const float ut = __fadd_rn(__fmul_rn(s1, ua), __fmul_rn(s0, ub));
+    const float ubm = __fadd_rn(__fmul_rn(s1, uc), __fmul_rn(s0, ud));
+    const float vt = __fadd_rn(__fmul_rn(s1, va), __fmul_rn(s0, vb));
+    const float vbm = __fadd_rn(__fmul_rn(s1, vc), __fmul_rn(s0, vd));
+    u[o] = su * __fadd_rn(__fmul_rn(s3, ut), __fmul_rn(s2, ubm));
+    v[o] = sv * __fadd_rn(__fmul_rn(s3, vt), __fmul_rn(s2, vbm));
+}
+
+__global__ void __launch_bounds__(256) splat_kernel(const float* __restrict__ d0, const float* __restrict__ u,
+                                                    const float* __restrict__ v, float* __restrict__ acc,
+                                                    const AdvectArgs A) {
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y + 1; i < A.rows - 1; i += blockDim.y * gridDim.y)
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j < A.cols - 1; j += blockDim.x * gridDim.x)
+            splat_cell(d0, u, v, acc, A, i, j);
+}
+
 __global__ void __launch_bounds__(256) density_finish_kernel(const float* __restrict__ acc, float* __restrict__ d,
                                                              int smooth, const AdvectArgs A, int* nonfinite) {
     int bad = 0;
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y) {
-        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x) {
-            float out = filled(acc, i, j, A);
-            if (smooth && i >= 1 && i <= A.rows - 2 && j >= 1 && j <= A.cols - 2) {
-                // 0.2f * (c + l + r + u + d), fluid_solver_gpu.cu:94
-                float s = __fadd_rn(out, filled(acc, i, j - 1, A));
-                s = __fadd_rn(s, filled(acc, i, j + 1, A));
-                s = __fadd_rn(s, filled(acc, i - 1, j, A));
-                s = __fadd_rn(s, filled(acc, i + 1, j, A));
-                out = __fmul_rn(0.2f, s);
-            }
-            d[(size_t)i * A.pitch + j] = out;
-            bad |= !isfinite(out);
-        }
-    }
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y)
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x)
+            bad |= finish_cell(acc, d, smooth, A, i, j);
     if (bad && nonfinite) atomicOr(nonfinite, 1);
 }
 
 __global__ void __launch_bounds__(256) advect_velocity_kernel(const float* __restrict__ u0,
                                                               const float* __restrict__ v0, float* __restrict__ u,
                                                               float* __restrict__ v, const AdvectArgs A) {
-    const size_t P = (size_t)A.pitch;
-    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y) {
-        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x) {
-            const bool ri = i >= 1 && i <= A.rows - 2, ci = j >= 1 && j <= A.cols - 2;
-            const size_t o = (size_t)i * P + j;
-            if (!ri && !ci) {  // corners are never written by the reference
-                u[o] = __ldg(u0 + o);
-                v[o] = __ldg(v0 + o);
-                continue;
-            }
-            // Edge cells copy the advected inner neighbour: u is negated on the
-            // left/right edges, v on the top/bottom edges (fluid_solver_gpu.cu:26-54).
-            int si = i, sj = j;
-            float su = 1.f, sv = 1.f;
-            if (!ci) {
-                sj = (j == 0) ? 1 : A.cols - 2;
-                su = -1.f;
-            } else if (!ri) {
-                si = (i == 0) ? 1 : A.rows - 2;
-                sv = -1.f;
-            }
-            const size_t so = (size_t)si * P + sj;
-            // advect_kernel, fluid_solver_gpu.cu:111-126
-            float x = __fsub_rn((float)sj, __fmul_rn(A.dt0, __ldg(u0 + so)));
-            float y = __fsub_rn((float)si, __fmul_rn(A.dt0, __ldg(v0 + so)));
-            x = fmaxf(1.5f, fminf(A.xmax, x));
-            y = fmaxf(1.5f, fminf(A.ymax, y));
-            const int j0 = (int)x, i0 = (int)y;
-            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
-            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
-            const size_t q = (size_t)i0 * P + j0;
-            const float ua = __ldg(u0 + q), ub = __ldg(u0 + q + 1), uc = __ldg(u0 + q + P), ud = __ldg(u0 + q + P + 1);
-            const float va = __ldg(v0 + q), vb = __ldg(v0 + q + 1), vc = __ldg(v0 + q + P), vd = __ldg(v0 + q + P + 1);
-            const float ut = __fadd_rn(__fmul_rn(s1, ua), __fmul_rn(s0, ub));
-            const float ubm = __fadd_rn(__fmul_rn(s1, uc), __fmul_rn(s0, ud));
-            const float vt = __fadd_rn(__fmul_rn(s1, va), __fmul_rn(s0, vb));
-            const float vbm = __fadd_rn(__fmul_rn(s1, vc), __fmul_rn(s0, vd));
-            u[o] = su * __fadd_rn(__fmul_rn(s3, ut), __fmul_rn(s2, ubm));
-            v[o] = sv * __fadd_rn(__fmul_rn(s3, vt), __fmul_rn(s2, vbm));
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < A.rows; i += blockDim.y * gridDim.y)
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.cols; j += blockDim.x * gridDim.x)
+            advect_cell(u0, v0, u, v, A, i, j);
+}
+
+// ----------------------------------------------------------------- batched
+// One launch covers every grid of a batch: blocks of 32x8 cells are numbered grid
+// by grid (prefix[g] = first block of grid g) and each block finds its grid by binary
+// search. Persistent: the launch has a few waves' worth of CTAs that stride over all
+// blocks.
+
+__device__ __forceinline__ int find_job(const int* __restrict__ prefix, int n, int b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int OP>
+__global__ void __launch_bounds__(256) advect_batch_kernel(const AdvectJob* __restrict__ jobs,
+                                                           const int* __restrict__ prefix, int njobs, int nblocks,
+                                                           int* nonfinite) {
+    int bad = 0;
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        const int g = find_job(prefix, njobs, b);
+        const AdvectJob& J = jobs[g];
+        const int lb = b - __ldg(prefix + g);
+        const int bx = (J.A.cols + 31) / 32;
+        const int i = (lb / bx) * 8 + threadIdx.y, j = (lb % bx) * 32 + threadIdx.x;
+        if (OP == 0) {
+            if (i >= 1 && i < J.A.rows - 1 && j >= 1 && j < J.A.cols - 1) splat_cell(J.in0, J.in1, J.in2, J.out0, J.A, i, j);
+        } else if (OP == 1) {
+            if (i < J.A.rows && j < J.A.cols) bad |= finish_cell(J.in0, J.out0, J.smooth, J.A, i, j);
+        } else {
+            if (i < J.A.rows && j < J.A.cols) advect_cell(J.in0, J.in1, J.out0, J.out1, J.A, i, j);
         }
     }
+    if (bad && nonfinite) atomicOr(nonfinite, 1);
 }
 
 dim3 grid_for(int rows, int cols) {
@@ -148,6 +204,21 @@ cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const 
 cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
                                    cudaStream_t st) {
     advect_velocity_kernel<<<grid_for(A.rows, A.cols), dim3(32, 8), 0, st>>>(u0, v0, u, v, A);
+    return cudaGetLastError();
+}
+
+int advect_batch_blocks(int rows, int cols) { return ((cols + 31) / 32) * ((rows + 7) / 8); }
+
+cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, int njobs, int nblocks,
+                                int* nonfinite, cudaStream_t st) {
+    if (nblocks <= 0) return cudaSuccess;
+    const int grid = std::min(nblocks, 152 * 8 * 4);
+    if (op == 0)
+        advect_batch_kernel<0><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
+    else if (op == 1)
+        advect_batch_kernel<1><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
+    else
+        advect_batch_kernel<2><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
     return cudaGetLastError();
 }
 

@@ -66,11 +66,50 @@ struct StencilLaunch {
     int nfields;
 };
 
+// Control block of one residual-driven pressure solve (device memory, cleared before
+// each solve): grid-barrier state, the barrier-timeout flag, and the outcome.
+struct SolveCtrl {
+    unsigned bar_count;
+    unsigned bar_gen;
+    int error;      // 1: a grid barrier gave up waiting (FS_ERR_TIMEOUT)
+    int passes;     // passes executed (each runs `sweeps` Jacobi sweeps)
+    int converged;  // 1: relative residual <= tol
+    int pad;
+    double residual;  // relative residual after the last executed pass
+};
+
+// A whole pressure solve run to a residual target by one persistent cooperative
+// launch: `first` (divergence fused) then `mid` passes until the relative residual
+// drops to tol or max_passes ran, then `fin` (zero sweeps: gradient subtract and
+// reflecting fills). Passes ping-pong between p[0] and p[1].
+struct PressureSolve {
+    StencilField first, mid, fin;
+    float* p[2];
+    float* p_out;      // receives the final pressure (warm start); may be null
+    double* partials;  // 4 doubles per CTA (residual sums, double-buffered by pass)
+    SolveCtrl* ctrl;
+    float tol;
+    int max_passes;
+};
+
 // Semi-Lagrangian advection parameters.
 struct AdvectArgs {
     int rows, cols, pitch;
     float dt0;          // sqrt(rows*cols)*dt (fluid_solver_gpu.cu:334)
     float xmax, ymax;   // cols-1.5f, rows-1.5f
+};
+
+// One grid's work in a batched advection launch. Splat: in0 = d0, in1 = u, in2 = v,
+// out0 = accumulator. Finish: in0 = accumulator, out0 = density. Velocity: in0 = u0,
+// in1 = v0, out0 = u, out1 = v.
+struct AdvectJob {
+    AdvectArgs A;
+    const float* in0;
+    const float* in1;
+    const float* in2;
+    float* out0;
+    float* out1;
+    int smooth;
 };
 
 // Tile geometry: tiles partition [0, n) starting at -shift, and never put a domain
@@ -89,10 +128,22 @@ int record_error(int code, const char* msg);
 cudaError_t stencil_prepare();
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st);
 int stencil_max_halo(int tile_rows);
+// Co-resident CTAs of the persistent pressure solve on the current device.
+cudaError_t pressure_solve_max_blocks(int tile_rows, int* blocks);
+cudaError_t launch_pressure_solve(const PressureSolve& P, int tile_rows, int blocks, cudaStream_t st);
 cudaError_t launch_splat(const float* d0, const float* u, const float* v, float* acc, const AdvectArgs& A,
                          cudaStream_t st);
 cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const AdvectArgs& A, int* nonfinite,
                                   cudaStream_t st);
+int advect_batch_blocks(int rows, int cols);
+// op 0: splat, 1: density finish, 2: velocity backtrace; prefix[g] = first 32x8
+// block of job g (njobs + 1 entries, the last = nblocks).
+cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, int njobs, int nblocks,
+                                int* nonfinite, cudaStream_t st);
+// Stencil pass over a device table of fields (batched grids); prefix[f] = first tile
+// of field f, prefix[nfields] = total tiles.
+cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, int nfields, int total_tiles,
+                                 bool diffuse, int tile_rows, cudaStream_t st);
 cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
                                    cudaStream_t st);
 

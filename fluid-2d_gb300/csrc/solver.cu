@@ -94,6 +94,11 @@ struct fs_solver {
     float* vel1[2] = {};
     float* pwarm[2] = {};
     int* flags = nullptr;  // [0]: non-finite
+    // residual-driven pressure solves: one control block per projection of a step,
+    // and the per-CTA residual partial sums of the persistent kernel
+    SolveCtrl* ctrl = nullptr;
+    double* partials[2] = {};
+    int solve_blocks = 0;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -249,8 +254,62 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
 
 // project (fluid_solver_gpu.cu:358-404): (u_in, v_in) -> (u_out, v_out). slot picks
 // the warm-start pressure buffer (the two projections of a step keep separate ones).
+// Residual-driven projection: one persistent cooperative launch runs depth-K passes
+// until the relative residual ||div + sum(nbrs) - 4p|| / ||div|| is <= tol or the
+// iteration cap is reached, then the gradient subtract (see pressure_solve_kernel).
+int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                                int slot, Counter& cnt) {
+    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    const float h = grid_h(s->rows, s->cols);
+    const int K = s->sweeps;
+    PressureSolve P{};
+    for (StencilField* f : {&P.first, &P.mid}) {
+        set_geometry(*f, s, K + 1);
+        f->s_lr = f->s_tb = 1.f;
+        f->sweeps = K;
+        f->cdiv = -0.5f * h;
+        f->h = h;
+    }
+    P.first.kind = PASS_PRESSURE_FIRST;
+    P.first.x = u_in;
+    P.first.x2 = v_in;
+    P.first.cst = (warm && s->warm_valid) ? s->pwarm[slot] : nullptr;
+    P.first.cst_out = s->div;
+    P.mid.kind = PASS_PRESSURE;
+    P.mid.cst = s->div;
+    StencilField& f = P.fin;
+    set_geometry(f, s, 1);
+    f.s_lr = f.s_tb = 1.f;
+    f.sweeps = 0;
+    f.h = h;
+    f.kind = PASS_PRESSURE;
+    f.cst = s->div;
+    f.epilogue = 1;
+    f.u_in = u_in;
+    f.v_in = v_in;
+    f.u_out = u_out;
+    f.v_out = v_out;
+    f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
+    P.p[0] = s->p[0];
+    P.p[1] = s->p[1];
+    P.p_out = warm ? s->pwarm[slot] : nullptr;
+    P.partials = s->partials[slot];
+    P.ctrl = s->ctrl + slot;
+    P.tol = s->cfg.pressure_tolerance;
+    P.max_passes = std::max(1, (s->cfg.pressure_max_iterations + K - 1) / K);
+    CK(cudaMemsetAsync(P.ctrl, 0, sizeof(SolveCtrl), s->stream));
+    const int blocks = std::min(s->solve_blocks, P.mid.tiles_x * P.mid.tiles_y);
+    PROF_BEGIN(s);
+    CK(launch_pressure_solve(P, s->tile_rows, blocks, s->stream));
+    PROF_END(s, FS_KIND_STENCIL, 0.0);  // bytes depend on the iteration count reached
+    cnt.launches++;
+    cnt.passes++;
+    return FS_OK;
+}
+
 int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out, int slot,
                     Counter& cnt) {
+    if (s->cfg.pressure_tolerance > 0.f) return enqueue_project_to_residual(s, u_in, v_in, u_out, v_out, slot, cnt);
     const std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
     const int m = (int)plan.size();
     const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
@@ -353,22 +412,29 @@ int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
     const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
     for (int k = 0; k < nsteps; ++k) {
         // The first warm-start step starts from zero pressure; its graph differs.
-        const bool graphable = s->cfg.use_graph && (!warm || s->warm_valid);
-        if (graphable) {
-            if (!s->graph_valid || diff != s->g_diff || visc != s->g_visc || dt != s->g_dt) {
-                destroy_graph(s);
-                Counter cnt;
-                CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-                rc = enqueue_step(s, diff, visc, dt, cnt);
-                cudaGraph_t g = nullptr;
-                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
-                if (rc != FS_OK) {
-                    if (g) cudaGraphDestroy(g);
-                    return rc;
+        bool graphable = s->cfg.use_graph && (!warm || s->warm_valid);
+        if (graphable && (!s->graph_valid || diff != s->g_diff || visc != s->g_visc || dt != s->g_dt)) {
+            destroy_graph(s);
+            Counter cnt;
+            CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_step(s, diff, visc, dt, cnt);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+            cudaGraphExec_t ge = nullptr;
+            if (rc == FS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+            if (rc != FS_OK || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                if (s->cfg.pressure_tolerance > 0.f) {
+                    // the runtime refused to capture the cooperative launch: step eagerly
+                    cudaGetLastError();
+                    s->cfg.use_graph = 0;
+                    graphable = false;
+                } else {
+                    return rc != FS_OK ? rc : cuda_fail(e, "step graph capture");
                 }
-                if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            } else {
                 s->graph = g;
-                CK(cudaGraphInstantiate(&s->gexec, g, 0));
+                s->gexec = ge;
                 s->graph_valid = true;
                 s->g_diff = diff;
                 s->g_visc = visc;
@@ -376,6 +442,8 @@ int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
                 s->launches_per_step = cnt.launches;
                 s->passes_per_step = cnt.passes;
             }
+        }
+        if (graphable) {
             CK(cudaGraphLaunch(s->gexec, s->stream));
             s->stats.kernel_launches += s->launches_per_step;
         } else {
@@ -391,15 +459,33 @@ int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
     return FS_OK;
 }
 
-int check_flags(fs_solver* s) {
-    if (!s->cfg.check_finite) return FS_OK;
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, s->flags, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+// Reads the residual solves' control blocks into the stats (blocking).
+int read_solve_ctrl(const fs_solver* s, SolveCtrl* out) {
+    CK(cudaMemcpyAsync(out, s->ctrl, 2 * sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    if (h) {
-        CK(cudaMemsetAsync(s->flags, 0, sizeof(int), s->stream));
-        s->stats.nonfinite = 1;
-        return fail(FS_ERR_NONFINITE, "the step produced a non-finite value");
+    return FS_OK;
+}
+
+int check_flags(fs_solver* s) {
+    if (s->cfg.check_finite) {
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, s->flags, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (h) {
+            CK(cudaMemsetAsync(s->flags, 0, sizeof(int), s->stream));
+            s->stats.nonfinite = 1;
+            return fail(FS_ERR_NONFINITE, "the step produced a non-finite value");
+        }
+    }
+    if (s->cfg.pressure_tolerance > 0.f && s->stats.steps > 0) {
+        SolveCtrl c[2];
+        int rc = read_solve_ctrl(s, c);
+        if (rc != FS_OK) return rc;
+        for (int k = 0; k < 2; ++k) {
+            if (c[k].error) return fail(FS_ERR_TIMEOUT, "pressure solve: a grid barrier timed out");
+            if (!c[k].converged)
+                return fail(FS_ERR_NOT_CONVERGED, "pressure solve: iteration cap reached before the residual target");
+        }
     }
     return FS_OK;
 }
@@ -460,7 +546,10 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         return fail(FS_ERR_ARG, "fs_create: unknown warm_start mode");
     if (cfg->tile_rows != 0 && cfg->tile_rows != 64 && cfg->tile_rows != 128)
         return fail(FS_ERR_ARG, "fs_create: tile_rows must be 0, 64 or 128");
-    if (cfg->pressure_tolerance > 0.f) return fail(FS_ERR_ARG, "fs_create: residual-driven pressure not enabled");
+    if (cfg->pressure_tolerance < 0.f || cfg->pressure_tolerance != cfg->pressure_tolerance)
+        return fail(FS_ERR_ARG, "fs_create: pressure_tolerance must be >= 0");
+    if (cfg->pressure_tolerance > 0.f && cfg->pressure_max_iterations < 1)
+        return fail(FS_ERR_ARG, "fs_create: pressure_max_iterations must be >= 1 with a residual target");
 
     fs_solver* s = new fs_solver();
     s->cfg = *cfg;
@@ -481,8 +570,18 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     const int maxk = stencil_max_halo(s->tile_rows) - 1;
     s->sweeps = cfg->sweeps_per_pass > 0 ? std::min(cfg->sweeps_per_pass, maxk) : std::min(8, maxk);
 
+    cudaError_t e = stencil_prepare();
+    if (e == cudaSuccess) e = pressure_solve_max_blocks(s->tile_rows, &s->solve_blocks);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(e, "fs_create: stencil kernel set-up");
+    }
     const int nfields = 6 + 9 + 6 + 2;
-    cudaError_t e = cudaMalloc(&s->slab, (size_t)nfields * s->field_floats * sizeof(float) + 256);
+    // tail: flags (256 B), two solve control blocks, two partial-sum arrays
+    const size_t part_doubles = 4 * (size_t)std::max(1, s->solve_blocks);
+    const size_t tail = 256 + 2 * 256 + 2 * part_doubles * sizeof(double);
+    const size_t slab_bytes = (size_t)nfields * s->field_floats * sizeof(float) + tail;
+    e = cudaMalloc(&s->slab, slab_bytes);
     if (e != cudaSuccess) {
         delete s;
         return cuda_fail(e, "fs_create: cudaMalloc");
@@ -508,14 +607,16 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     s->vel1[1] = take();
     s->pwarm[0] = take();
     s->pwarm[1] = take();
-    s->flags = reinterpret_cast<int*>(p);
+    char* tailp = reinterpret_cast<char*>(p);
+    s->flags = reinterpret_cast<int*>(tailp);
+    s->ctrl = reinterpret_cast<SolveCtrl*>(tailp + 256);
+    s->partials[0] = reinterpret_cast<double*>(tailp + 256 + 2 * 256);
+    s->partials[1] = s->partials[0] + part_doubles;
     int rc = FS_OK;
-    if ((e = cudaMemset(s->slab, 0, (size_t)nfields * s->field_floats * sizeof(float) + 256)) != cudaSuccess)
+    if ((e = cudaMemset(s->slab, 0, slab_bytes)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaMemset");
     else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaStreamCreate");
-    else if ((e = stencil_prepare()) != cudaSuccess)
-        rc = cuda_fail(e, "fs_create: stencil kernel attributes");
     if (rc != FS_OK) {
         if (s->stream) cudaStreamDestroy(s->stream);
         cudaFree(s->slab);
@@ -683,6 +784,16 @@ int fs_get_stats(const fs_solver* s, fs_stats* out) {
     out->sweeps_per_pass = s->sweeps;
     out->tile_rows = s->tile_rows;
     out->pressure_iterations_last[0] = out->pressure_iterations_last[1] = s->cfg.pressure_iterations;
+    if (s->cfg.pressure_tolerance > 0.f && s->stats.steps > 0) {
+        DeviceGuard g(s->device);
+        SolveCtrl c[2];
+        int rc = read_solve_ctrl(s, c);
+        if (rc != FS_OK) return rc;
+        for (int k = 0; k < 2; ++k) {
+            out->pressure_iterations_last[k] = c[k].passes * s->sweeps;
+            out->pressure_residual_last[k] = c[k].residual;
+        }
+    }
     return FS_OK;
 }
 

@@ -26,6 +26,8 @@
 // where the reference's double rounding lands exactly on a float tie (about one
 // value in 10^8 in random testing).
 
+#include <algorithm>
+
 #include "fs_internal.cuh"
 
 namespace fs {
@@ -53,19 +55,52 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
     return __fmul_rn(s, 0.25f);
 }
 
-template <int TY, int SR>
-__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
-    stencil_kernel(const __grid_constant__ StencilLaunch L) {
-    constexpr int RW = kRegionW, RH = TY * SR;
-    extern __shared__ float4 smem4[];
-    float* cur = reinterpret_cast<float*>(smem4);
-    float* nxt = cur + RH * RW;
+// One Jacobi sweep of a thread's column strip (SR rows). Neighbours above/below the
+// strip and left/right come from `cur` (the previous sweep), the strip itself from
+// registers; results go to registers and `nxt`.
+//   ROWCHK: rows outside [lo, hi) (the sweep's dependency cone, or outside the domain
+//           interior) are skipped; rows are shared by the whole warp, so this is a
+//           uniform branch.
+//   COLCHK: lanes whose column is not domain-interior keep their value (only CTAs on
+//           the domain edge need this).
+template <bool DIFF, bool ROWCHK, bool COLCHK, int SR, int RH>
+__device__ __forceinline__ void sweep_strip(float (&c)[SR], const float (&k)[SR], const float* __restrict__ cur,
+                                            float* __restrict__ nxt, int r0, int tx, int txl, int txr,
+                                            bool col_int, int lo, int hi, float a, float dh, float dl, float rf) {
+    constexpr int RW = kRegionW;
+    float up = (r0 > 0) ? cur[(r0 - 1) * RW + tx] : c[0];
+#pragma unroll
+    for (int i = 0; i < SR; ++i) {
+        const int r = r0 + i;
+        const float old = c[i];
+        if (!ROWCHK || (r >= lo && r < hi)) {
+            float down;
+            if (i + 1 < SR)
+                down = c[i + 1];
+            else
+                down = (r + 1 < RH) ? cur[(r + 1) * RW + tx] : c[i];
+            const float Lv = cur[r * RW + txl], Rv = cur[r * RW + txr];
+            float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, down, a, dh, dl, rf)
+                            : pressure_update(k[i], Lv, Rv, up, down);
+            if (COLCHK) nv = col_int ? nv : old;
+            c[i] = nv;
+            nxt[r * RW + tx] = nv;
+        }
+        up = old;
+    }
+}
 
-    int b = blockIdx.x, f = 0;
-#pragma unroll 1
-    while (f + 1 < L.nfields && b >= L.f[f + 1].tile_begin) ++f;
-    const StencilField& F = L.f[f];
-    b -= F.tile_begin;
+// One tile of one pass: load the region (fusing add_sources or the divergence into
+// the first pass), run F.sweeps sweeps with the boundary fill after each, store the
+// output tile, then the optional gradient-subtract epilogue and the optional residual
+// partial sums (for residual-driven pressure solves). xin/yout stand in for F.x/F.y so
+// a persistent caller can ping-pong buffers across passes.
+template <int TY, int SR, bool DIFF>
+__device__ __forceinline__ void process_tile(const StencilField& F, int b, const float* __restrict__ xin,
+                                             float* __restrict__ yout, float* cur, float* nxt, bool resid,
+                                             float& rnum, float& rden) {
+    constexpr int RW = kRegionW, RH = TY * SR;
+    __syncthreads();  // the previous tile of this CTA may still be reading shared memory
     const int tyi = b / F.tiles_x, txi = b - tyi * F.tiles_x;
     const int H = F.halo;
     const int gy0 = tyi * F.tile_h - F.shift_y - H;
@@ -91,8 +126,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             const int gr = gy0 + r0 + i;
             const bool in = col_in && gr >= 0 && gr < rows;
             const size_t o = (size_t)gr * pitch + gc;
-            cur[(r0 + i) * RW + tx] = in ? __ldg(F.x + o) : 0.f;
-            nxt[(r0 + i) * RW + tx] = in ? __ldg(F.x2 + o) : 0.f;
+            cur[(r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
+            nxt[(r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
         }
         __syncthreads();
         const float cdiv = F.cdiv;
@@ -106,7 +141,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             const bool interior = col_int && gr >= 1 && gr <= rows - 2;
             k[i] = interior ? __fmul_rn(cdiv, s) : 0.f;
             const bool in = col_in && gr >= 0 && gr < rows;
-            c[i] = (F.cst != nullptr && in) ? __ldg(F.cst + (size_t)gr * pitch + gc) : 0.f;
+            c[i] = (F.cst != nullptr && in) ? __ldcg(F.cst + (size_t)gr * pitch + gc) : 0.f;
         }
         __syncthreads();
     } else if (kind == PASS_DIFFUSE_FIRST) {
@@ -118,8 +153,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             const bool in = col_in && gr >= 0 && gr < rows;
             const bool interior = col_int && gr >= 1 && gr <= rows - 2;
             const size_t o = (size_t)gr * pitch + gc;
-            float x = in ? __ldg(F.x + o) : 0.f;
-            if (interior) x = __fadd_rn(x, __fmul_rn(dt, __ldg(F.x2 + o)));
+            float x = in ? __ldcg(xin + o) : 0.f;
+            if (interior) x = __fadd_rn(x, __fmul_rn(dt, __ldcg(F.x2 + o)));
             c[i] = x;
             k[i] = x;
         }
@@ -130,8 +165,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             const bool in = col_in && gr >= 0 && gr < rows;
             const bool interior = col_int && gr >= 1 && gr <= rows - 2;
             const size_t o = (size_t)gr * pitch + gc;
-            c[i] = in ? __ldg(F.x + o) : 0.f;
-            k[i] = interior ? __ldg(F.cst + o) : 0.f;
+            c[i] = in ? __ldcg(xin + o) : 0.f;
+            k[i] = interior ? __ldcg(F.cst + o) : 0.f;
         }
     }
 #pragma unroll
@@ -139,33 +174,25 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
-    const bool diffuse = (kind == PASS_DIFFUSE_FIRST || kind == PASS_DIFFUSE);
     const float a = F.a, dh = F.dh, dl = F.dl, rf = F.rf;
     const float s_lr = F.s_lr, s_tb = F.s_tb;
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
+    // region rows that are domain-interior: [row_lo, row_hi)
+    const int row_lo = max(0, 1 - gy0), row_hi = min(RH, rows - 1 - gy0);
     const int nsweeps = F.sweeps;
 #pragma unroll 1
     for (int s = 0; s < nsweeps; ++s) {
-        float up = (r0 > 0) ? cur[(r0 - 1) * RW + tx] : c[0];
-#pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i, gr = gy0 + r;
-            float down;
-            if (i + 1 < SR)
-                down = c[i + 1];
-            else
-                down = (r + 1 < RH) ? cur[(r + 1) * RW + tx] : c[i];
-            const float Lv = cur[r * RW + txl], Rv = cur[r * RW + txr];
-            const float old = c[i];
-            const bool interior = col_int && gr >= 1 && gr <= rows - 2;
-            float nv = old;
-            if (interior)
-                nv = diffuse ? diffuse_update(k[i], Lv, Rv, up, down, a, dh, dl, rf)
-                             : pressure_update(k[i], Lv, Rv, up, down);
-            c[i] = nv;
-            nxt[r * RW + tx] = nv;
-            up = old;
-        }
+        // Rows that the output (plus its ring, when an epilogue needs one) depends on
+        // after this sweep: [s+1, RH-1-s), intersected with the domain interior.
+        // Rows outside keep stale values that nothing downstream reads.
+        const int lo = max(s + 1, row_lo), hi = min(RH - 1 - s, row_hi);
+        if (edge_cta)
+            sweep_strip<DIFF, true, true, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl, rf);
+        else if (r0 >= lo && r0 + SR <= hi)
+            sweep_strip<DIFF, false, false, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl,
+                                                    rf);
+        else
+            sweep_strip<DIFF, true, false, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl, rf);
         __syncthreads();
         if (edge_cta) {
             // set_boundary_* (fluid_solver_gpu.cu:11-54): edges from the new inner
@@ -209,57 +236,253 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             const int r = r0 + i, gr = gy0 + r;
             if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
             const size_t o = (size_t)gr * pitch + gc;
-            if (F.y) F.y[o] = c[i];
+            if (yout) yout[o] = c[i];
             if (F.cst_out) F.cst_out[o] = k[i];
         }
     }
-    if (!F.epilogue || !col_out) return;
+    if (F.epilogue && col_out) {
 
-    // ---------------------------------------------- gradient subtract epilogue
-    // remove_p_kernel (fluid_solver_gpu.cu:202-203) then the reflecting fills
-    // set_boundary_opposite_horizontal(u) / _vertical(v) (fluid_solver_gpu.cu:402-403).
-    // Edge cells take the updated value of their inner neighbour (negated for the
-    // normal component), corners keep their input value.
-    const float h = F.h;
-    int bad = 0;
-#pragma unroll
-    for (int i = 0; i < SR; ++i) {
-        const int r = r0 + i, gr = gy0 + r;
-        if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
-        const bool row_int = gr >= 1 && gr <= rows - 2;
-        int ir = gr, ic = gc;
-        float su = 1.f, sv = 1.f;
-        bool corner = false;
-        if (col_int && row_int) {
-        } else if (row_int) {  // left / right edge
-            ic = (gc == 0) ? 1 : cols - 2;
-            su = -1.f;
-        } else if (col_int) {  // top / bottom edge
-            ir = (gr == 0) ? 1 : rows - 2;
-            sv = -1.f;
-        } else {
-            corner = true;
+        // ---------------------------------------------- gradient subtract epilogue
+        // remove_p_kernel (fluid_solver_gpu.cu:202-203) then the reflecting fills
+        // set_boundary_opposite_horizontal(u) / _vertical(v) (fluid_solver_gpu.cu:402-403).
+        // Edge cells take the updated value of their inner neighbour (negated for the
+        // normal component), corners keep their input value.
+        const float h = F.h;
+        int bad = 0;
+    #pragma unroll
+        for (int i = 0; i < SR; ++i) {
+            const int r = r0 + i, gr = gy0 + r;
+            if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
+            const bool row_int = gr >= 1 && gr <= rows - 2;
+            int ir = gr, ic = gc;
+            float su = 1.f, sv = 1.f;
+            bool corner = false;
+            if (col_int && row_int) {
+            } else if (row_int) {  // left / right edge
+                ic = (gc == 0) ? 1 : cols - 2;
+                su = -1.f;
+            } else if (col_int) {  // top / bottom edge
+                ir = (gr == 0) ? 1 : rows - 2;
+                sv = -1.f;
+            } else {
+                corner = true;
+            }
+            const size_t o = (size_t)gr * pitch + gc;
+            float un, vn;
+            if (corner) {
+                un = __ldcg(F.u_in + o);
+                vn = __ldcg(F.v_in + o);
+            } else {
+                const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
+                const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
+                const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
+                const float gu = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rr * RW + rcr], cur[rr * RW + rcl])), h);
+                const float gv = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rrd * RW + rc], cur[rru * RW + rc])), h);
+                const size_t oi = (size_t)ir * pitch + ic;
+                un = su * __fsub_rn(__ldcg(F.u_in + oi), gu);
+                vn = sv * __fsub_rn(__ldcg(F.v_in + oi), gv);
+            }
+            F.u_out[o] = un;
+            F.v_out[o] = vn;
+            bad |= !(isfinite(un) && isfinite(vn));
         }
-        const size_t o = (size_t)gr * pitch + gc;
-        float un, vn;
-        if (corner) {
-            un = __ldg(F.u_in + o);
-            vn = __ldg(F.v_in + o);
-        } else {
-            const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
-            const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
-            const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
-            const float gu = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rr * RW + rcr], cur[rr * RW + rcl])), h);
-            const float gv = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rrd * RW + rc], cur[rru * RW + rc])), h);
-            const size_t oi = (size_t)ir * pitch + ic;
-            un = su * __fsub_rn(__ldg(F.u_in + oi), gu);
-            vn = sv * __fsub_rn(__ldg(F.v_in + oi), gv);
-        }
-        F.u_out[o] = un;
-        F.v_out[o] = vn;
-        bad |= !(isfinite(un) && isfinite(vn));
+        if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
     }
-    if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
+
+    // ------------------------------------------------ residual partial sums
+    // ||div + sum(nbrs) - 4p||^2 and ||div||^2 over this tile's interior output
+    // cells, from the final p (valid one ring beyond the tile: halo = sweeps + 1).
+    if (resid && col_out) {
+#pragma unroll
+        for (int i = 0; i < SR; ++i) {
+            const int r = r0 + i, gr = gy0 + r;
+            if (r < H || r >= H + F.tile_h || !col_int || gr < 1 || gr > rows - 2) continue;
+            const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
+            float sres = k[i] + cur[r * RW + txr];
+            sres += cur[r * RW + txl];
+            sres += cur[rd * RW + tx];
+            sres += cur[ru * RW + tx];
+            const float res = sres - 4.f * c[i];
+            rnum = fmaf(res, res, rnum);
+            rden = fmaf(k[i], k[i], rden);
+        }
+    }
+}
+
+// One launch = one pass over the tiles of up to kMaxStencilFields fields.
+template <int TY, int SR, bool DIFF>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+    stencil_kernel(const __grid_constant__ StencilLaunch L) {
+    constexpr int RH = TY * SR;
+    extern __shared__ float4 smem4[];
+    float* cur = reinterpret_cast<float*>(smem4);
+    float* nxt = cur + RH * kRegionW;
+    int b = blockIdx.x, f = 0;
+#pragma unroll 1
+    while (f + 1 < L.nfields && b >= L.f[f + 1].tile_begin) ++f;
+    const StencilField& F = L.f[f];
+    float rn = 0.f, rd = 0.f;
+    process_tile<TY, SR, DIFF>(F, b - F.tile_begin, F.x, F.y, cur, nxt, false, rn, rd);
+}
+
+// One pass over a device-resident table of fields (a batch of grids of uneven
+// size). Persistent: a few CTAs per SM stride over the concatenated tile list;
+// prefix[f] is the first tile of field f and each tile finds its field by binary
+// search. Tiles of all grids have the same shape, so the stride keeps SMs balanced.
+template <int TY, int SR, bool DIFF>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+    stencil_table_kernel(const StencilField* __restrict__ tab, const int* __restrict__ prefix, int nf, int total) {
+    constexpr int RH = TY * SR;
+    extern __shared__ float4 smem4[];
+    float* cur = reinterpret_cast<float*>(smem4);
+    float* nxt = cur + RH * kRegionW;
+#pragma unroll 1
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int lo = 0, hi = nf - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(prefix + mid) <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const StencilField& F = tab[lo];
+        float rn = 0.f, rd = 0.f;
+        process_tile<TY, SR, DIFF>(F, t - __ldg(prefix + lo), F.x, F.y, cur, nxt, false, rn, rd);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual-driven pressure solve in one persistent cooperative launch.
+
+constexpr unsigned kBarrierSpinLimit = 1u << 24;  // ~2 s of polling, then give up
+
+// Grid-wide barrier for a cooperative launch (all CTAs co-resident). The wait is
+// bounded: after kBarrierSpinLimit polls the CTA sets ctrl->error and continues, and
+// every later barrier returns at once, so the kernel always terminates. Returns false
+// once an error has been flagged.
+__device__ __forceinline__ bool grid_barrier(SolveCtrl* ctrl, unsigned nblocks) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        volatile unsigned* gen = &ctrl->bar_gen;
+        volatile int* err = &ctrl->error;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&ctrl->bar_count, 1u) == nblocks - 1) {
+            atomicExch(&ctrl->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctrl->bar_gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*gen == g && *err == 0) {
+                if (++spins > kBarrierSpinLimit) {
+                    atomicExch(&ctrl->error, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = (*err == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Fixed-order block sum of two doubles (shuffle tree, then warps in order); every
+// thread receives the result.
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+    __shared__ double sa[32], sb[32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nw = (blockDim.x * blockDim.y + 31) / 32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    __syncthreads();
+    if ((tid & 31) == 0) {
+        sa[tid >> 5] = a;
+        sb[tid >> 5] = b;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double x = 0, y = 0;
+        for (int w = 0; w < nw; ++w) {
+            x += sa[w];
+            y += sb[w];
+        }
+        sa[0] = x;
+        sb[0] = y;
+    }
+    __syncthreads();
+    a = sa[0];
+    b = sb[0];
+}
+
+// Out-of-line tile call for the persistent kernel: keeps the pass loop's state out
+// of the tile body's register budget.
+template <int TY, int SR>
+__device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, float* cur,
+                                           float* nxt, bool resid, float& rn, float& rd) {
+    process_tile<TY, SR, false>(F, t, x, y, cur, nxt, resid, rn, rd);
+}
+
+template <int TY, int SR>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+    pressure_solve_kernel(const __grid_constant__ PressureSolve P) {
+    constexpr int RH = TY * SR;
+    extern __shared__ float4 smem4[];
+    float* cur = reinterpret_cast<float*>(smem4);
+    float* nxt = cur + RH * kRegionW;
+    const unsigned G = gridDim.x;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    const int ntiles = P.mid.tiles_x * P.mid.tiles_y;
+    int passes = 0;
+    double ratio = 0.0;
+    bool ok = true;
+#pragma unroll 1
+    for (int pass = 0; pass < P.max_passes; ++pass) {
+        const StencilField& F = pass == 0 ? P.first : P.mid;
+        const float* x = pass == 0 ? F.x : P.p[(pass - 1) & 1];
+        float rn = 0.f, rd = 0.f;
+#pragma unroll 1
+        for (int t = blockIdx.x; t < ntiles; t += G)
+            pressure_tile<TY, SR>(F, t, x, P.p[pass & 1], cur, nxt, true, rn, rd);
+        double a = rn, b = rd;
+        block_sum2(a, b);
+        double* part = P.partials + (size_t)(pass & 1) * 2 * G;
+        if (tid == 0) {
+            part[2 * blockIdx.x] = a;
+            part[2 * blockIdx.x + 1] = b;
+        }
+        ok = grid_barrier(P.ctrl, G);
+        passes = pass + 1;
+        if (!ok) break;
+        // every CTA sums all partials in the same order, so all agree on the outcome
+        a = 0.0;
+        b = 0.0;
+        for (unsigned i = tid; i < G; i += nt) {
+            a += __ldcg(part + 2 * i);
+            b += __ldcg(part + 2 * i + 1);
+        }
+        block_sum2(a, b);
+        ratio = b > 0.0 ? sqrt(a / b) : sqrt(a);
+        if (ratio <= (double)P.tol) break;
+    }
+    if (ok) {
+        // gradient subtract + reflecting fills from the final pressure
+        const int nfin = P.fin.tiles_x * P.fin.tiles_y;
+        const float* pf = P.p[(passes - 1) & 1];
+        float rn = 0.f, rd = 0.f;
+#pragma unroll 1
+        for (int t = blockIdx.x; t < nfin; t += G)
+            pressure_tile<TY, SR>(P.fin, t, pf, P.p_out, cur, nxt, false, rn, rd);
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        P.ctrl->passes = passes;
+        P.ctrl->residual = ratio;
+        P.ctrl->converged = ok && ratio <= (double)P.tol;
+    }
 }
 
 template <int TY, int SR>
@@ -269,8 +492,68 @@ constexpr size_t smem_bytes() {
 
 template <int TY, int SR>
 cudaError_t prepare_variant() {
-    return cudaFuncSetAttribute(stencil_kernel<TY, SR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_bytes<TY, SR>());
+    const int smem = (int)smem_bytes<TY, SR>();
+    cudaError_t e = cudaFuncSetAttribute(stencil_kernel<TY, SR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(stencil_kernel<TY, SR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pressure_solve_kernel<TY, SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+    return e;
+}
+
+template <int TY, int SR>
+cudaError_t launch_table_variant(const StencilField* tab, const int* prefix, int nf, int total, bool diffuse,
+                                 cudaStream_t st) {
+    if (total <= 0) return cudaSuccess;
+    int dev = 0, sms = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stencil_table_kernel<TY, SR, false>, kRegionW * TY,
+                                                          smem_bytes<TY, SR>());
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(total, per * sms));
+    if (diffuse)
+        stencil_table_kernel<TY, SR, true><<<grid, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix, nf,
+                                                                                                    total);
+    else
+        stencil_table_kernel<TY, SR, false><<<grid, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix, nf,
+                                                                                                     total);
+    return cudaGetLastError();
+}
+
+template <int TY, int SR>
+cudaError_t solve_blocks(int* blocks) {
+    int dev = 0, sms = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pressure_solve_kernel<TY, SR>, kRegionW * TY,
+                                                          smem_bytes<TY, SR>());
+    *blocks = per * sms;
+    return e;
+}
+
+template <int TY, int SR>
+cudaError_t launch_solve_variant(const PressureSolve& P, int blocks, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kRegionW, TY);
+    cfg.dynamicSmemBytes = smem_bytes<TY, SR>();
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, pressure_solve_kernel<TY, SR>, P);
 }
 
 template <int TY, int SR>
@@ -279,7 +562,12 @@ cudaError_t launch_variant(const StencilLaunch& L, cudaStream_t st) {
     int blocks = 0;
     for (int i = 0; i < L.nfields; ++i) blocks += L.f[i].tiles_x * L.f[i].tiles_y;
     if (blocks == 0) return cudaSuccess;
-    stencil_kernel<TY, SR><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
+    // all fields of one launch are of the same class (diffusion or pressure)
+    const bool diff = L.f[0].kind == PASS_DIFFUSE_FIRST || L.f[0].kind == PASS_DIFFUSE;
+    if (diff)
+        stencil_kernel<TY, SR, true><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
+    else
+        stencil_kernel<TY, SR, false><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
     return cudaGetLastError();
 }
 
@@ -298,6 +586,23 @@ cudaError_t stencil_prepare() {
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st) {
     if (tile_rows == 128) return launch_variant<8, 16>(L, st);
     return launch_variant<4, 16>(L, st);
+}
+
+cudaError_t pressure_solve_max_blocks(int tile_rows, int* blocks) {
+    if (tile_rows == 128) return solve_blocks<8, 16>(blocks);
+    return solve_blocks<4, 16>(blocks);
+}
+
+cudaError_t launch_pressure_solve(const PressureSolve& P, int tile_rows, int blocks, cudaStream_t st) {
+    if (blocks <= 0) return cudaErrorInvalidValue;
+    if (tile_rows == 128) return launch_solve_variant<8, 16>(P, blocks, st);
+    return launch_solve_variant<4, 16>(P, blocks, st);
+}
+
+cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, int nfields, int total_tiles,
+                                 bool diffuse, int tile_rows, cudaStream_t st) {
+    if (tile_rows == 128) return launch_table_variant<8, 16>(table, prefix, nfields, total_tiles, diffuse, st);
+    return launch_table_variant<4, 16>(table, prefix, nfields, total_tiles, diffuse, st);
 }
 
 }  // namespace fs

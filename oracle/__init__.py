@@ -34,6 +34,8 @@ def lib():
         L = C.CDLL(str(path))
         L.orc_gpu_solve_f32.argtypes = [_L, _L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I, _I]
         L.orc_gpu_solve_f64.argtypes = [_L, _L, _f64p, _f64p, _F, _f64p, _f64p, _f64p, _f64p, _F, _F, _I, _I, _I, _I]
+        L.orc_gpu_solve_ex_f32.argtypes = [_L, _L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I,
+                                           _I, C.c_void_p, C.c_void_p]
         L.orc_cpu_solve_f32.argtypes = [_L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I]
         L.orc_add_sources_f32.argtypes = [_L, _L, _f32p, _f32p, _F]
         L.orc_diffuse_f32.argtypes = [_L, _L, _f32p, _I, _F, _F, _I]
@@ -84,6 +86,21 @@ def gpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=15, kp=20, smooth=True, ns
     d, ds, u, v, us, vs = (_c(a, t) for a in (d, ds, u, v, us, vs))
     fn = lib().orc_gpu_solve_f64 if f64 else lib().orc_gpu_solve_f32
     _chk(fn(d.shape[0], d.shape[1], d, ds, diff, u, v, us, vs, visc, dt, kd, kp, int(smooth), nsteps))
+    return d, u, v
+
+
+def gpu_solve_ex(d, ds, diff, u, v, us, vs, visc, dt, kd, kp1, kp2, smooth=True, pw=None):
+    """One step with separate sweep counts for the two projections. pw = [p1, p2]
+    float32 arrays used as starting pressures and overwritten with the final ones
+    (previous-pressure warm start); None starts both from zero."""
+    d, ds, u, v, us, vs = (_c(a) for a in (d, ds, u, v, us, vs))
+    p1 = pw[0].ctypes.data if pw is not None else None
+    p2 = pw[1].ctypes.data if pw is not None else None
+    if pw is not None:
+        for a in pw:
+            assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] and a.shape == d.shape
+    _chk(lib().orc_gpu_solve_ex_f32(d.shape[0], d.shape[1], d, ds, diff, u, v, us, vs, visc, dt, kd, kp1, kp2,
+                                    int(smooth), p1, p2))
     return d, u, v
 
 

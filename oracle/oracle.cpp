@@ -226,7 +226,28 @@ template <class T> void gpu_project(Field<T> u, Field<T> v, int iters, T* p_inou
 }
 
 // fluid_solver_gpu::solve, fluid_solver_gpu.cu:222-258, with the iteration counts
-// as parameters (the reference uses kd = 15, kp = 20).
+// as parameters (the reference uses kd = 15, kp = 20). kp1/kp2 are the sweeps of the
+// two projections; pw1/pw2 (nullable) are their starting pressures in and final
+// pressures out (the previous-pressure warm start; null = start from zero).
+template <class T>
+void gpu_solve_ex(long R, long C, T* d, const T* ds, float diff, T* u, T* v, const T* us, const T* vs,
+                  float visc, float dt, int kd, int kp1, int kp2, int smooth, T* pw1, T* pw2) {
+    Field<T> D{d, R, C}, U{u, R, C}, V{v, R, C};
+    gpu_add_sources(D, ds, dt);
+    gpu_diffuse(D, BND_CONT, diff, dt, kd);
+    gpu_advect_trace(D, u, v, dt);
+    if (smooth) gpu_smooth(D);
+    gpu_add_sources(U, us, dt);
+    gpu_add_sources(V, vs, dt);
+    gpu_diffuse(U, BND_OPP_H, visc, dt, kd);
+    gpu_diffuse(V, BND_OPP_V, visc, dt, kd);
+    gpu_project(U, V, kp1, pw1, (T*)nullptr);
+    std::vector<T> u0(u, u + R * C), v0(v, v + R * C);
+    gpu_advect_gather(U, u0.data(), u0.data(), v0.data(), BND_OPP_H, dt);
+    gpu_advect_gather(V, v0.data(), u0.data(), v0.data(), BND_OPP_V, dt);
+    gpu_project(U, V, kp2, pw2, (T*)nullptr);
+}
+
 template <class T>
 void gpu_solve(long R, long C, T* d, const T* ds, float diff, T* u, T* v, const T* us, const T* vs,
                float visc, float dt, int kd, int kp, int smooth) {
@@ -441,6 +462,15 @@ int orc_gpu_solve_f64(long rows, long cols, double* d, const double* ds, float d
                       int smooth, int nsteps) {
     if (bad(rows, cols)) return 1;
     for (int s = 0; s < nsteps; ++s) gpu_solve<double>(rows, cols, d, ds, diff, u, v, us, vs, visc, dt, kd, kp, smooth);
+    return 0;
+}
+
+// One step with separate projection sweep counts and optional warm-start pressures.
+int orc_gpu_solve_ex_f32(long rows, long cols, float* d, const float* ds, float diff, float* u, float* v,
+                         const float* us, const float* vs, float visc, float dt, int kd, int kp1, int kp2,
+                         int smooth, float* pw1, float* pw2) {
+    if (bad(rows, cols)) return 1;
+    gpu_solve_ex<float>(rows, cols, d, ds, diff, u, v, us, vs, visc, dt, kd, kp1, kp2, smooth, pw1, pw2);
     return 0;
 }
 

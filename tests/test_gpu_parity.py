@@ -216,3 +216,54 @@ def test_shape_and_dtype_checks(fluid):
             s.solve(bad, ok, 0.0, ok, ok, ok, ok, 0.0, 0.1)
         with pytest.raises(TypeError):
             s.solve(ok.astype(np.float64), ok, 0.0, ok, ok, ok, ok, 0.0, 0.1)
+
+
+def test_previous_pressure_warm_start(fluid, wl):
+    """Each projection starts from its own final pressure of the previous step."""
+    w = wl.small_sources(64, seed=12)
+    d, u, v = w.state()
+    od, ou, ov = w.state()
+    pw = [np.zeros((w.rows, w.cols), np.float32) for _ in range(2)]
+    with make_solver(fluid, w.rows, w.cols, warm_start=fluid.FS_WARM_PREVIOUS) as s:
+        for _ in range(8):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            od, ou, ov = oracle.gpu_solve_ex(od, w.ds, w.diffusion, ou, ov, w.us, w.vs, w.viscosity, w.dt, 15, 20, 20,
+                                             pw=pw)
+            for g, o in ((d, od), (u, ou), (v, ov)):
+                assert oracle.rel_linf(g, o) <= TOL
+
+
+@pytest.mark.parametrize("warm", [0, 1])
+@pytest.mark.parametrize("sweeps,tile_rows", [(8, 64), (5, 128)])
+def test_residual_mode_equals_oracle_at_the_same_sweeps(fluid, wl, warm, sweeps, tile_rows):
+    """Residual-driven projections: the GPU reports how many sweeps each projection
+    took; the oracle run with exactly those sweeps must give the same fields."""
+    w = wl.small_sources(80, seed=13)
+    tol = 2e-3
+    d, u, v = w.state()
+    od, ou, ov = w.state()
+    pw = [np.zeros((w.rows, w.cols), np.float32) for _ in range(2)] if warm else None
+    with make_solver(fluid, w.rows, w.cols, pressure_tolerance=tol, pressure_max_iterations=20000,
+                     sweeps_per_pass=sweeps, tile_rows=tile_rows, warm_start=warm) as s:
+        for _ in range(4):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            st = s.stats()
+            k1, k2 = st["pressure_iterations_last"]
+            assert k1 % sweeps == 0 and k2 % sweeps == 0 and k1 > 0 and k2 > 0
+            assert max(st["pressure_residual_last"]) <= tol
+            od, ou, ov = oracle.gpu_solve_ex(od, w.ds, w.diffusion, ou, ov, w.us, w.vs, w.viscosity, w.dt, 15, k1, k2,
+                                             pw=pw)
+            for g, o in ((d, od), (u, ou), (v, ov)):
+                assert oracle.rel_linf(g, o) <= TOL
+
+
+def test_residual_mode_reports_the_iteration_cap(fluid, wl):
+    w = wl.small_sources(40, seed=14)
+    d, u, v = w.state()
+    with make_solver(fluid, w.rows, w.cols, pressure_tolerance=1e-9, pressure_max_iterations=16,
+                     sweeps_per_pass=8) as s:
+        with pytest.raises(fluid.FluidError) as e:
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+        assert e.value.code == fluid.FS_ERR_NOT_CONVERGED
+        assert s.stats()["pressure_iterations_last"] == [16, 16]
+        assert np.isfinite(d).all() and np.isfinite(u).all()
