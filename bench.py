@@ -36,6 +36,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -56,6 +58,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--workload", choices=("vortex", "small", "batch", "residual"), default="vortex",
+                    help="vortex: the default 2048^2 line; small: 130^2 with sources, 20/20 sweeps; "
+                         "batch: 256 uneven grids, 30/30 sweeps, batch vs looped handles; "
+                         "residual: pressure to a relative-residual target")
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--max-iters", type=int, default=2000)
+    ap.add_argument("--count", type=int, default=256)
+    ap.add_argument("--tune", action="store_true", help="autotune the tiling before timing")
     return ap.parse_args()
 
 
@@ -161,6 +171,7 @@ def cpu_baseline(w, kd, kp, budget_s=15.0):
 def run_reference(a):
     """Reference arm: fluid_solver_cpu (Gauss-Seidel) restated in the oracle and pinned
     bit-exactly against the compiled reference; single-threaded like the reference."""
+    __graft_entry__.load_package()
     import oracle
     from fluid2d_gb300 import workloads
 
@@ -346,12 +357,179 @@ def run_ours(a):
         torch.distributed.destroy_process_group()
 
 
+def _timed_steps(step, sync, stream, steps, flush_l2, torch, dev):
+    """CUDA-event time of `steps` calls of step(), L2 flushed before each."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for k in range(steps):
+        flush_l2()
+        evs[k][0].record(stream)
+        step()
+        evs[k][1].record(stream)
+    sync()
+    torch.cuda.synchronize(dev)
+    return sum(e0.elapsed_time(e1) for e0, e1 in evs)
+
+
+def run_small(a):
+    """130x130 (N=128) with 4 density and 4 velocity sources, dt 0.1, rates 1e-4,
+    20/20 sweeps, the reference's own CPU-runnable case."""
+    import torch
+
+    pkg = __graft_entry__.load_package()
+    from fluid2d_gb300 import workloads
+
+    w = workloads.small_sources(128, seed=1)
+    s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=20, device=0, check_finite=0)
+    s.upload(*w.state())
+    s.upload_sources(*w.sources())
+    stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
+    s.step(w.diffusion, w.viscosity, w.dt, nsteps=a.warmup)
+    ms = _timed_steps(lambda: s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False), s.sync, stream, a.steps,
+                      lambda: None, torch, 0)
+    line = {"metric": metric_name(), "value": w.interior_cells * a.steps / (ms / 1e3), "unit": "cell-steps/s",
+            "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded sources)",
+            "config": {"workload": "small_sources 128x128 interior, 20/20 sweeps, dt 0.1, rates 1e-4",
+                       "l2": "not flushed (working set 1.5 MB)", **{k: v for k, v in s.stats().items()
+                                                                    if k in ("launches_per_step", "passes_per_step")}}}
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
+def run_batch(a):
+    """256 independent grids, N uniform in {64..1024}, 30/30 sweeps: one fs_batch
+    (one launch per sub-step, graph per step) vs the same grids as 256 handles."""
+    import torch
+
+    pkg = __graft_entry__.load_package()
+    from fluid2d_gb300 import build_lib, workloads
+
+    build_lib.build()
+    kd = kp = 30
+    sims = workloads.batch(a.count, seed=4, kd=kd, kp=kp)
+    shapes = [(w.rows, w.cols) for w in sims]
+    cells = sum(w.interior_cells for w in sims)
+    w0 = sims[0]
+    cfg = dict(diffuse_iterations=kd, pressure_iterations=kp, device=0, check_finite=0)
+    if a.sweeps:
+        cfg["sweeps_per_pass"] = a.sweeps
+    if a.tile_rows:
+        cfg["tile_rows"] = a.tile_rows
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=0)
+    b = pkg.Batch(shapes, **cfg)
+    for k, w in enumerate(sims):
+        b.upload(k, *w.state())
+        b.upload_sources(k, *w.sources())
+    stream = torch.cuda.ExternalStream(b.stream, device=0)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    b.step(w0.diffusion, w0.viscosity, w0.dt, nsteps=a.warmup)
+    l0 = b.stats()["kernel_launches"]
+    ms_b = _timed_steps(lambda: b.step(w0.diffusion, w0.viscosity, w0.dt, 1, sync=False), b.sync, stream, a.steps,
+                        flush_l2, torch, 0)
+    launches = b.stats()["kernel_launches"] - l0
+    st = b.stats()
+    b.close()
+    # the same grids as independent handles, stepped one after another per step
+    hs = []
+    for w in sims:
+        s = pkg.Solver(w.rows, w.cols, **cfg)
+        s.upload(*w.state())
+        s.upload_sources(*w.sources())
+        s.step(w.diffusion, w.viscosity, w.dt, nsteps=1)
+        hs.append(s)
+    streams = [torch.cuda.ExternalStream(h.device_view().stream, device=0) for h in hs]
+    steps_l = max(2, a.steps // 4)
+    torch.cuda.synchronize(0)
+    t0 = time.perf_counter()
+    for _ in range(steps_l):
+        for h in hs:
+            h.step(w0.diffusion, w0.viscosity, w0.dt, 1, sync=False)
+        for h in hs:
+            h.sync()
+    ms_l = (time.perf_counter() - t0) * 1e3
+    for h in hs:
+        h.close()
+    line = {"metric": metric_name(), "value": cells * a.steps / (ms_b / 1e3), "unit": "cell-steps/s", "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_b / a.steps, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded vortex fields + sources)", "gpu_launches": launches,
+            "config": {"workload": f"batch of {len(sims)} grids, N uniform in 64..1024, Kd=Kp=30, dt 0.05",
+                       "interior_cells": cells, "launches_per_step": st["launches_per_step"],
+                       "sweeps_per_pass": st["sweeps_per_pass"], "tile_rows": st["tile_rows"],
+                       "l2": "flushed between timed steps"},
+            "looped_handles": {"value": cells * steps_l / (ms_l / 1e3), "ms_per_step": ms_l / steps_l,
+                               "timing": "host wall clock, one graph per handle per step"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_residual(a):
+    """Pressure solves run to a relative residual target (the to-residual mode), with
+    zero or previous-pressure warm start; reports sweeps used per projection."""
+    import torch
+
+    pkg = __graft_entry__.load_package()
+    from fluid2d_gb300 import build_lib, workloads
+
+    build_lib.build()
+    w = workloads.vortex_field(a.size, seed=2, kd=a.kd, kp=a.kp)
+    out = []
+    for warm in (0, 1):
+        cfg = dict(diffuse_iterations=a.kd, pressure_tolerance=a.tol, pressure_max_iterations=a.max_iters,
+                   warm_start=warm, device=0, check_finite=0)
+        if a.sweeps:
+            cfg["sweeps_per_pass"] = a.sweeps
+        if a.tile_rows:
+            cfg["tile_rows"] = a.tile_rows
+        s = pkg.Solver(w.rows, w.cols, **cfg)
+        s.upload(*w.state())
+        s.upload_sources(*w.sources())
+        stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
+        iters, res, ms_tot = [], [], 0.0
+        for k in range(a.warmup + a.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False)
+            e1.record(stream)
+            try:
+                s.sync()
+            except pkg.FluidError as e:
+                if e.code != pkg.FS_ERR_NOT_CONVERGED:
+                    raise
+            st = s.stats()
+            if k >= a.warmup:
+                ms_tot += e0.elapsed_time(e1)
+                iters.append(st["pressure_iterations_last"])
+                res.append(st["pressure_residual_last"])
+        out.append({"warm_start": ["zero", "previous"][warm], "ms_per_step": ms_tot / a.steps,
+                    "sweeps_per_projection_mean": float(np.mean(iters)), "sweeps_max": int(np.max(iters)),
+                    "residual_max": float(np.max(res)), "capped_projections": int(np.sum(np.array(iters) >= a.max_iters)),
+                    "sweeps_per_pass": s.stats()["sweeps_per_pass"], "tile_rows": s.stats()["tile_rows"]})
+        s.close()
+    line = {"metric": "ms/step to relative pressure residual", "unit": "ms/step", "higher_is_better": False,
+            "value": out[1]["ms_per_step"], "steps": a.steps, "warmup": a.warmup, "dtype": "f32",
+            "data": "synthetic (seeded vortex field)",
+            "config": {"workload": f"vortex_field {a.size}^2, pressure to {a.tol:g} relative residual, "
+                                   f"cap {a.max_iters} sweeps, Kd={a.kd}"},
+            "modes": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     if a.warmup < 3:
         a.warmup = 3
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "small":
+        run_small(a)
+    elif a.workload == "batch":
+        run_batch(a)
+    elif a.workload == "residual":
+        run_residual(a)
     else:
         run_ours(a)
 

@@ -85,6 +85,16 @@ SIGNATURES = {
     "fs_stage": (C.c_int, [_P, _I, _F, _F]),
     "fs_profile_step": (C.c_int, [_P, _F, _F, _F, C.POINTER(fs_kernel_times)]),
     "fs_project_noalloc": (C.c_int, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "fs_batch_create": (C.c_int, [C.POINTER(fs_config), _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P)]),
+    "fs_batch_destroy": (C.c_int, [_P]),
+    "fs_batch_upload": (C.c_int, [_P, _I, _P, _P, _P]),
+    "fs_batch_upload_sources": (C.c_int, [_P, _I, _P, _P, _P]),
+    "fs_batch_step": (C.c_int, [_P, _F, _F, _F, _I]),
+    "fs_batch_download": (C.c_int, [_P, _I, _P, _P, _P]),
+    "fs_batch_sync": (C.c_int, [_P]),
+    "fs_batch_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
+    "fs_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "fs_autotune": (C.c_int, [C.POINTER(fs_config), _F, _F, _F, _I, C.c_char_p, C.POINTER(C.c_double)]),
     "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
     "fs_host_free": (C.c_int, [_P]),
     "fs_version": (C.c_char_p, []),
@@ -132,6 +142,17 @@ def default_config(rows: int, cols: int, **kw) -> fs_config:
             raise AttributeError(f"unknown config field {k}")
         setattr(cfg, k, v)
     return cfg
+
+
+def autotune(rows, cols, diffusion_rate, viscosity, dt, steps=5, cache_path=None, **config) -> dict:
+    """Pick tile_rows / sweeps_per_pass for this grid and sweep plan by timing steps on
+    the device (fs_autotune). Returns the chosen fields and the time per step."""
+    L = load()
+    cfg = default_config(rows, cols, **config)
+    ms = C.c_double()
+    path = str(cache_path).encode() if cache_path else None
+    _check(L.fs_autotune(C.byref(cfg), diffusion_rate, viscosity, dt, steps, path, C.byref(ms)))
+    return {"tile_rows": cfg.tile_rows, "sweeps_per_pass": cfg.sweeps_per_pass, "ms_per_step": ms.value}
 
 
 class Solver:
@@ -228,6 +249,86 @@ class Solver:
     @property
     def handle(self):
         return self._h
+
+
+class Batch:
+    """Many independent grids of uneven size stepped together (fs_batch_*)."""
+
+    def __init__(self, shapes, **config):
+        self._lib = load()
+        self.shapes = [(int(r), int(c)) for r, c in shapes]
+        self.config = default_config(3, 3, **config)
+        n = len(self.shapes)
+        rows = (C.c_int * n)(*[r for r, _ in self.shapes])
+        cols = (C.c_int * n)(*[c for _, c in self.shapes])
+        h = C.c_void_p()
+        _check(self._lib.fs_batch_create(C.byref(self.config), n, rows, cols, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.shapes)
+
+    def _shape(self, k, *arrs):
+        for a in arrs:
+            if a.shape != self.shapes[k]:
+                raise ValueError(f"grid {k}: shape {a.shape} != {self.shapes[k]}")
+
+    def upload(self, k, d, u, v):
+        self._shape(k, d, u, v)
+        _check(self._lib.fs_batch_upload(self._h, k, _ptr(d), _ptr(u), _ptr(v)))
+        _check(self._lib.fs_batch_sync(self._h))
+
+    def upload_sources(self, k, ds, us, vs):
+        self._shape(k, ds, us, vs)
+        _check(self._lib.fs_batch_upload_sources(self._h, k, _ptr(ds), _ptr(us), _ptr(vs)))
+        _check(self._lib.fs_batch_sync(self._h))
+
+    def step(self, diffusion_rate, viscosity, dt, nsteps=1, sync=True):
+        _check(self._lib.fs_batch_step(self._h, diffusion_rate, viscosity, dt, nsteps))
+        if sync:
+            _check(self._lib.fs_batch_sync(self._h))
+
+    def sync(self):
+        _check(self._lib.fs_batch_sync(self._h))
+
+    def download(self, k):
+        r, c = self.shapes[k]
+        d = np.empty((r, c), np.float32)
+        u = np.empty_like(d)
+        v = np.empty_like(d)
+        _check(self._lib.fs_batch_download(self._h, k, _ptr(d, True), _ptr(u, True), _ptr(v, True)))
+        _check(self._lib.fs_batch_sync(self._h))
+        return d, u, v
+
+    def stats(self) -> dict:
+        st = fs_stats()
+        _check(self._lib.fs_batch_get_stats(self._h, C.byref(st)))
+        return {"steps": st.steps, "kernel_launches": st.kernel_launches,
+                "launches_per_step": st.launches_per_step, "passes_per_step": st.passes_per_step,
+                "sweeps_per_pass": st.sweeps_per_pass, "tile_rows": st.tile_rows}
+
+    @property
+    def stream(self):
+        p = C.c_void_p()
+        _check(self._lib.fs_batch_stream(self._h, C.byref(p)))
+        return p.value
 
 
 class FluidSolverGPU(Solver):

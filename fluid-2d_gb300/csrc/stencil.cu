@@ -55,38 +55,73 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
     return __fmul_rn(s, 0.25f);
 }
 
-// One Jacobi sweep of a thread's column strip (SR rows). Neighbours above/below the
-// strip and left/right come from `cur` (the previous sweep), the strip itself from
-// registers; results go to registers and `nxt`.
-//   ROWCHK: rows outside [lo, hi) (the sweep's dependency cone, or outside the domain
-//           interior) are skipped; rows are shared by the whole warp, so this is a
-//           uniform branch.
-//   COLCHK: lanes whose column is not domain-interior keep their value (only CTAs on
-//           the domain edge need this).
-template <bool DIFF, bool ROWCHK, bool COLCHK, int SR, int RH>
-__device__ __forceinline__ void sweep_strip(float (&c)[SR], const float (&k)[SR], const float* __restrict__ cur,
-                                            float* __restrict__ nxt, int r0, int tx, int txl, int txr,
-                                            bool col_int, int lo, int hi, float a, float dh, float dl, float rf) {
+// All sweeps of one tile. Each thread owns one column of SR rows: its values and its
+// constant term (x0 or div) live in registers; horizontal neighbours and the rows just
+// above/below the strip come from `cur` (the previous sweep), new values go to
+// registers and `nxt`, one barrier per sweep.
+//   EDGE = false: the region lies inside the domain interior; every cell updates, no
+//                 checks (cells near the region border compute values that nothing
+//                 stored depends on).
+//   EDGE = true:  bit i of `live` marks interior cells; after each sweep the domain-edge
+//                 cells take their inner neighbour's new value (set_boundary_*,
+//                 fluid_solver_gpu.cu:11-54): etop/ebot mark top/bottom edge cells,
+//                 eside left/right edge cells (neighbour column side_src); corners keep
+//                 their value.
+template <bool DIFF, bool EDGE, int SR, int RH>
+__device__ __forceinline__ void run_sweeps(float (&c)[SR], const float (&k)[SR], float*& cur, float*& nxt,
+                                           int nsweeps, int r0, int tx, int txl, int txr, unsigned live, int gy0,
+                                           int gc, int rows, int cols, float s_lr, float s_tb, float a, float dh,
+                                           float dl, float rf) {
     constexpr int RW = kRegionW;
-    float up = (r0 > 0) ? cur[(r0 - 1) * RW + tx] : c[0];
+#pragma unroll 1
+    for (int s = 0; s < nsweeps; ++s) {
+        const float* __restrict__ cr = cur;
+        float* __restrict__ nx = nxt;
+        float up = (r0 > 0) ? cr[(r0 - 1) * RW + tx] : c[0];
+        const float dn = (r0 + SR < RH) ? cr[(r0 + SR) * RW + tx] : c[SR - 1];
 #pragma unroll
-    for (int i = 0; i < SR; ++i) {
-        const int r = r0 + i;
-        const float old = c[i];
-        if (!ROWCHK || (r >= lo && r < hi)) {
-            float down;
-            if (i + 1 < SR)
-                down = c[i + 1];
-            else
-                down = (r + 1 < RH) ? cur[(r + 1) * RW + tx] : c[i];
-            const float Lv = cur[r * RW + txl], Rv = cur[r * RW + txr];
+        for (int i = 0; i < SR; ++i) {
+            const float old = c[i];
+            const float down = (i + 1 < SR) ? c[i + 1] : dn;
+            const float Lv = cr[(r0 + i) * RW + txl], Rv = cr[(r0 + i) * RW + txr];
             float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, down, a, dh, dl, rf)
                             : pressure_update(k[i], Lv, Rv, up, down);
-            if (COLCHK) nv = col_int ? nv : old;
+            if (EDGE) nv = ((live >> i) & 1u) ? nv : old;
             c[i] = nv;
-            nxt[r * RW + tx] = nv;
+            nx[(r0 + i) * RW + tx] = nv;
+            up = old;
         }
-        up = old;
+        __syncthreads();
+        if (EDGE) {
+            const bool col_int = gc >= 1 && gc <= cols - 2;
+#pragma unroll
+            for (int i = 0; i < SR; ++i) {
+                const int r = r0 + i, gr = gy0 + r;
+                float val;
+                if (col_int) {
+                    if (gr == 0)
+                        val = s_tb * nx[min(r + 1, RH - 1) * RW + tx];
+                    else if (gr == rows - 1)
+                        val = s_tb * nx[max(r - 1, 0) * RW + tx];
+                    else
+                        continue;
+                } else if (gr >= 1 && gr <= rows - 2) {
+                    if (gc == 0)
+                        val = s_lr * nx[r * RW + txr];
+                    else if (gc == cols - 1)
+                        val = s_lr * nx[r * RW + txl];
+                    else
+                        continue;
+                } else {
+                    continue;
+                }
+                c[i] = val;
+                nx[r * RW + tx] = val;
+            }
+            __syncthreads();
+        }
+        cur = nx;
+        nxt = const_cast<float*>(cr);
     }
 }
 
@@ -174,58 +209,19 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
-    const float a = F.a, dh = F.dh, dl = F.dl, rf = F.rf;
-    const float s_lr = F.s_lr, s_tb = F.s_tb;
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
-    // region rows that are domain-interior: [row_lo, row_hi)
-    const int row_lo = max(0, 1 - gy0), row_hi = min(RH, rows - 1 - gy0);
-    const int nsweeps = F.sweeps;
-#pragma unroll 1
-    for (int s = 0; s < nsweeps; ++s) {
-        // Rows that the output (plus its ring, when an epilogue needs one) depends on
-        // after this sweep: [s+1, RH-1-s), intersected with the domain interior.
-        // Rows outside keep stale values that nothing downstream reads.
-        const int lo = max(s + 1, row_lo), hi = min(RH - 1 - s, row_hi);
-        if (edge_cta)
-            sweep_strip<DIFF, true, true, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl, rf);
-        else if (r0 >= lo && r0 + SR <= hi)
-            sweep_strip<DIFF, false, false, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl,
-                                                    rf);
-        else
-            sweep_strip<DIFF, true, false, SR, RH>(c, k, cur, nxt, r0, tx, txl, txr, col_int, lo, hi, a, dh, dl, rf);
-        __syncthreads();
-        if (edge_cta) {
-            // set_boundary_* (fluid_solver_gpu.cu:11-54): edges from the new inner
-            // neighbour, corners untouched.
+    if (edge_cta) {
+        unsigned live = 0;
 #pragma unroll
-            for (int i = 0; i < SR; ++i) {
-                const int r = r0 + i, gr = gy0 + r;
-                float val;
-                if (col_int) {
-                    if (gr == 0)
-                        val = s_tb * nxt[(r < RH - 1 ? r + 1 : r) * RW + tx];
-                    else if (gr == rows - 1)
-                        val = s_tb * nxt[(r > 0 ? r - 1 : r) * RW + tx];
-                    else
-                        continue;
-                } else if (gr >= 1 && gr <= rows - 2) {
-                    if (gc == 0)
-                        val = s_lr * nxt[r * RW + txr];
-                    else if (gc == cols - 1)
-                        val = s_lr * nxt[r * RW + txl];
-                    else
-                        continue;
-                } else {
-                    continue;
-                }
-                c[i] = val;
-                nxt[r * RW + tx] = val;
-            }
-            __syncthreads();
+        for (int i = 0; i < SR; ++i) {
+            const int gr = gy0 + r0 + i;
+            live |= (unsigned)(col_int && gr >= 1 && gr <= rows - 2) << i;
         }
-        float* t = cur;
-        cur = nxt;
-        nxt = t;
+        run_sweeps<DIFF, true, SR, RH>(c, k, cur, nxt, F.sweeps, r0, tx, txl, txr, live, gy0, gc, rows, cols,
+                                       F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf);
+    } else {
+        run_sweeps<DIFF, false, SR, RH>(c, k, cur, nxt, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
+                                        F.s_tb, F.a, F.dh, F.dl, F.rf);
     }
 
     // ------------------------------------------------------------------ store

@@ -1,0 +1,137 @@
+// Autotuner for the stencil tiling: picks the region height (tile_rows) and the
+// temporal-blocking depth (sweeps_per_pass) for one grid shape and sweep plan by
+// timing whole steps on the device, and caches the choice in a text file.
+//
+// No counterpart in the reference, whose launch shape is fixed (32x32 blocks,
+// kernel_launcher.hpp:14-16, 28-30) and whose sweep counts are hard-coded.
+//
+// Cache file: one line per key,
+//   <device name>|<SMs>|<rows>|<cols>|<kd>|<kp>|<tol>|<warm> <tile_rows> <sweeps> <ms>
+// Later lines win, so a re-tune appends.
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host_common.h"
+
+using namespace fs;
+
+namespace {
+
+std::string tune_key(const fs_config* c) {
+    int dev = c->device;
+    if (dev < 0) cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    std::memset(&prop, 0, sizeof(prop));
+    cudaGetDeviceProperties(&prop, dev);
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s|%d|%d|%d|%d|%d|%g|%d", prop.name, prop.multiProcessorCount, c->rows, c->cols,
+                  c->diffuse_iterations, c->pressure_iterations, (double)c->pressure_tolerance, c->warm_start);
+    for (char* p = buf; *p; ++p)
+        if (*p == ' ') *p = '_';
+    return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& key, int* tile_rows, int* sweeps, double* ms) {
+    if (!path) return false;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return false;
+    char k[512];
+    int tr, sw;
+    double t;
+    bool found = false;
+    while (std::fscanf(f, "%511s %d %d %lf", k, &tr, &sw, &t) == 4) {
+        if (key == k) {
+            *tile_rows = tr;
+            *sweeps = sw;
+            *ms = t;
+            found = true;
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+void cache_store(const char* path, const std::string& key, int tile_rows, int sweeps, double ms) {
+    if (!path) return;
+    FILE* f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%s %d %d %.6f\n", key.c_str(), tile_rows, sweeps, ms);
+    std::fclose(f);
+}
+
+// Mean milliseconds per step of `cfg` on a zero state with the given physics.
+int time_config(const fs_config* cfg, float diff, float visc, float dt, int steps, double* ms) {
+    fs_solver* s = nullptr;
+    int rc = fs_create(cfg, &s);
+    if (rc != FS_OK) return rc;
+    fs_device_view v;
+    fs_device_view_get(s, &v);
+    cudaStream_t st = (cudaStream_t)v.stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    rc = fs_step(s, diff, visc, dt, 2);  // warm-up (captures the graph)
+    if (rc == FS_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        rc = record_error(FS_ERR_CUDA, "fs_autotune: cudaEventCreate");
+    if (rc == FS_OK) {
+        cudaEventRecord(e0, st);
+        rc = fs_step(s, diff, visc, dt, steps);
+        cudaEventRecord(e1, st);
+    }
+    if (rc == FS_OK) rc = fs_sync(s);
+    if (rc == FS_OK || rc == FS_ERR_NOT_CONVERGED) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        *ms = t / steps;
+        rc = FS_OK;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    fs_destroy(s);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int fs_autotune(fs_config* cfg, float diffusion_rate, float viscosity, float dt, int steps,
+                           const char* cache_path, double* best_ms) {
+    if (!cfg || steps < 1) return record_error(FS_ERR_ARG, "fs_autotune: bad argument");
+    DeviceScope scope(cfg->device);
+    const std::string key = tune_key(cfg);
+    int tr = 0, sw = 0;
+    double ms = 0.0;
+    if (cache_lookup(cache_path, key, &tr, &sw, &ms)) {
+        cfg->tile_rows = tr;
+        cfg->sweeps_per_pass = sw;
+        if (best_ms) *best_ms = ms;
+        return FS_OK;
+    }
+    const int heights[2] = {64, 128};
+    const int depths[7] = {4, 6, 8, 10, 12, 14, 16};
+    double best = 1e30;
+    int best_tr = 0, best_sw = 0;
+    for (int h : heights) {
+        for (int d : depths) {
+            if (d > stencil_max_halo(h) - 1) continue;
+            fs_config c = *cfg;
+            c.tile_rows = h;
+            c.sweeps_per_pass = d;
+            double t = 0.0;
+            int rc = time_config(&c, diffusion_rate, viscosity, dt, steps, &t);
+            if (rc != FS_OK) return rc;
+            if (t < best) {
+                best = t;
+                best_tr = h;
+                best_sw = d;
+            }
+        }
+    }
+    cfg->tile_rows = best_tr;
+    cfg->sweeps_per_pass = best_sw;
+    if (best_ms) *best_ms = best;
+    cache_store(cache_path, key, best_tr, best_sw, best);
+    return FS_OK;
+}

@@ -164,7 +164,7 @@ def batch(count=256, seed=4, kd=30, kp=30, dt=0.05, rate=1e-5):
     for k, N in enumerate(batch_sizes(count, seed)):
         n = N + 2
         scale = N / 2048.0
-        cnt = max(1, int(round(64 * scale * scale * 4)))
+        cnt = max(2, int(round(16 * (N / 1024.0) ** 2)))
         u, v = vortex_velocity(n, n, cnt, seed * 1000 + k, max(3.0, 20 * scale * 2), max(6.0, 80 * scale * 2))
         d = lowfreq_noise(n, n, seed * 1000 + k + 500)
         rng = np.random.default_rng(seed * 7919 + k)

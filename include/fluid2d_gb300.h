@@ -136,6 +136,33 @@ FS_API int fs_device_view_get(fs_solver* s, fs_device_view* out);
 #define FS_STAGE_ADVECT_VELOCITY 5  /* backtrace advection of u, v (fluid_solver_gpu.cu:248-251) */
 FS_API int fs_stage(fs_solver* s, int stage, float rate, float dt);
 
+/* Autotuner: times whole steps of candidate stencil tilings (region height 64/128 x
+ * blocking depth 4..16) for cfg's grid and sweep plan on the device and writes the
+ * fastest into cfg->tile_rows / cfg->sweeps_per_pass. With a cache_path the choice is
+ * looked up first and stored after tuning (key: device, SM count, rows, cols, kd, kp,
+ * tolerance, warm start). No counterpart in the reference (fixed 32x32 launches,
+ * kernel_launcher.hpp:14-16). best_ms (nullable) receives the time per step. */
+FS_API int fs_autotune(fs_config* cfg, float diffusion_rate, float viscosity, float dt, int steps,
+                       const char* cache_path, double* best_ms);
+
+/* Batches: many independent grids of uneven size advanced together. No counterpart
+ * in the reference (which steps one grid per fluid_solver_gpu object). Every sub-step
+ * of the step is one launch over all grids; the step is replayed as a CUDA graph.
+ * Grids share dt, the rates, the sweep counts and the config (cfg->rows/cols are
+ * ignored; rows[k], cols[k] give grid k, boundary included). Residual-driven pressure
+ * and warm starts are not available for batches. */
+typedef struct fs_batch fs_batch;
+FS_API int fs_batch_create(const fs_config* cfg, int count, const int* rows, const int* cols, fs_batch** out);
+FS_API int fs_batch_destroy(fs_batch* b);
+FS_API int fs_batch_upload(fs_batch* b, int index, const float* density, const float* u, const float* v);
+FS_API int fs_batch_upload_sources(fs_batch* b, int index, const float* density_source, const float* u_source,
+                                   const float* v_source);
+FS_API int fs_batch_step(fs_batch* b, float diffusion_rate, float viscosity, float dt, int nsteps);
+FS_API int fs_batch_download(fs_batch* b, int index, float* density, float* u, float* v);
+FS_API int fs_batch_sync(fs_batch* b);
+FS_API int fs_batch_get_stats(const fs_batch* b, fs_stats* out);
+FS_API int fs_batch_stream(fs_batch* b, void** stream);
+
 /* Per-kernel timing of one step. The step runs eagerly (not from the graph) with a
  * CUDA event recorded on the handle's stream around every launch; for each kernel kind
  * the result holds the launch count, the summed event time and the algorithmic bytes
