@@ -58,7 +58,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=3)
-    ap.add_argument("--workload", choices=("vortex", "small", "batch", "residual"), default="vortex",
+    ap.add_argument("--samples", type=int, default=20000, help="learned: training pairs")
+    ap.add_argument("--epochs", type=int, default=8, help="learned: training epochs")
+    ap.add_argument("--weights", default="", help="learned: save trained parameters here (.npy)")
+    ap.add_argument("--load-weights", default="", help="learned: skip training and load parameters")
+    ap.add_argument("--eval-sizes", default="1024,2048")
+    ap.add_argument("--tols", default="1e-1,3e-2,1e-2,1e-4")
+    ap.add_argument("--workload", choices=("vortex", "small", "batch", "residual", "learned"), default="vortex",
                     help="vortex: the default 2048^2 line; small: 130^2 with sources, 20/20 sweeps; "
                          "batch: 256 uneven grids, 30/30 sweeps, batch vs looped handles; "
                          "residual: pressure to a relative-residual target")
@@ -518,6 +524,83 @@ def run_residual(a):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(a):
+    """Learned pressure warm start: train on (divergence, exact pressure) pairs from
+    seeded 512^2 vortex runs, then step vortex fields at the evaluation sizes with the
+    pressure solved to each residual target from (i) the previous pressure and (ii) the
+    network's correction of it; report sweeps per projection, ms/step and how often
+    the solver fell back to the previous pressure."""
+    import torch
+
+    pkg = __graft_entry__.load_package()
+    from fluid2d_gb300 import build_lib, learned, train_warmstart, workloads
+
+    build_lib.build()
+    info = {}
+    if a.load_weights:
+        params = np.load(a.load_weights).astype(np.float32)
+    else:
+        t0 = time.perf_counter()
+        X, T, ginfo = train_warmstart.generate(a.samples, size=512, steps_per_run=200, seed=100)
+        t1 = time.perf_counter()
+        params, hist = train_warmstart.train(X, T, epochs=a.epochs, batch=128, lr=1e-3, seed=0)
+        t2 = time.perf_counter()
+        base = train_warmstart.evaluate_loss(learned.init_params(0), X[:2048], T[:2048])
+        fin = train_warmstart.evaluate_loss(params, X[:2048], T[:2048])
+        info = {"samples": int(X.shape[0]), "gen_s": t1 - t0, "train_s": t2 - t1, "epochs": a.epochs,
+                "loss_init": base, "loss_trained": fin, "loss_first_batch": hist[0], "loss_last_batch": hist[-1]}
+        if a.weights:
+            np.save(a.weights, params)
+        del X, T
+        torch.cuda.empty_cache()
+    results = []
+    for size in [int(x) for x in a.eval_sizes.split(",")]:
+        w = workloads.vortex_field(size, seed=3, kd=a.kd, kp=a.kp)
+        for tol in [float(x) for x in a.tols.split(",")]:
+            row = {"size": size, "tol": tol}
+            for mode, warm in (("previous", pkg.FS_WARM_PREVIOUS), ("learned", pkg.FS_WARM_LEARNED)):
+                s = pkg.Solver(w.rows, w.cols, diffuse_iterations=a.kd, pressure_tolerance=tol,
+                               pressure_max_iterations=a.max_iters, warm_start=warm, device=0, check_finite=0)
+                if warm == pkg.FS_WARM_LEARNED:
+                    s.set_network(params)
+                s.upload(*w.state())
+                s.upload_sources(*w.sources())
+                stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
+                sweeps, res, ms = [], [], 0.0
+                for k in range(a.warmup + a.steps):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False)
+                    e1.record(stream)
+                    try:
+                        s.sync()
+                    except pkg.FluidError as e:
+                        if e.code != pkg.FS_ERR_NOT_CONVERGED:
+                            raise
+                    st = s.stats()
+                    if k >= a.warmup:
+                        ms += e0.elapsed_time(e1)
+                        sweeps += st["pressure_iterations_last"]
+                        res += st["pressure_residual_last"]
+                st = s.stats()
+                row[mode] = {"ms_per_step": ms / a.steps, "sweeps_per_projection": float(np.mean(sweeps)),
+                             "capped": int(np.sum(np.array(sweeps) >= a.max_iters)),
+                             "residual_max": float(np.max(res))}
+                if warm == pkg.FS_WARM_LEARNED:
+                    used, fb = st["learned_used"], st["learned_fallback"]
+                    row[mode]["fallback_rate"] = fb / max(1, used + fb)
+                s.close()
+            row["speedup_ms"] = row["previous"]["ms_per_step"] / row["learned"]["ms_per_step"]
+            results.append(row)
+            print(json.dumps(row), flush=True)
+    line = {"metric": "ms/step to relative pressure residual, learned vs previous-pressure warm start",
+            "unit": "ms/step", "higher_is_better": False, "steps": a.steps, "warmup": a.warmup, "dtype": "f32",
+            "data": "synthetic (seeded vortex fields)", "training": info, "results": results,
+            "config": {"workload": f"vortex_field {a.eval_sizes}, Kd={a.kd}, cap {a.max_iters} sweeps",
+                       "network": "8 conv layers 3x3x32, BF16 tcgen05 implicit GEMM, 32x32 coarse grid"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
     if a.warmup < 3:
@@ -530,6 +613,8 @@ def main():
         run_batch(a)
     elif a.workload == "residual":
         run_residual(a)
+    elif a.workload == "learned":
+        run_learned(a)
     else:
         run_ours(a)
 

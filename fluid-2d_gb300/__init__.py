@@ -15,6 +15,7 @@ without the built library raises. Build it with ``build_lib.build()`` (or
 from __future__ import annotations
 
 import ctypes as C
+import os
 import pathlib
 
 import numpy as np
@@ -23,7 +24,7 @@ from . import build_lib
 
 FS_OK, FS_ERR_ARG, FS_ERR_CUDA, FS_ERR_NONFINITE, FS_ERR_NOT_CONVERGED, FS_ERR_TIMEOUT, FS_ERR_NOMEM, \
     FS_ERR_STATE = range(8)
-FS_WARM_ZERO, FS_WARM_PREVIOUS = 0, 1
+FS_WARM_ZERO, FS_WARM_PREVIOUS, FS_WARM_LEARNED = 0, 1, 2
 STAGE_DIFFUSE_DENSITY, STAGE_ADVECT_DENSITY, STAGE_DIFFUSE_VELOCITY, STAGE_PROJECT, STAGE_ADVECT_VELOCITY = 1, 2, 3, 4, 5
 
 LIB_PATH = build_lib.LIB
@@ -40,14 +41,14 @@ class fs_config(C.Structure):
                 ("pressure_iterations", C.c_int), ("smooth", C.c_int), ("sweeps_per_pass", C.c_int),
                 ("tile_rows", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("warm_start", C.c_int),
                 ("pressure_tolerance", C.c_float), ("pressure_max_iterations", C.c_int),
-                ("check_finite", C.c_int)]
+                ("check_finite", C.c_int), ("capture", C.c_int)]
 
 
 class fs_stats(C.Structure):
     _fields_ = [("steps", C.c_longlong), ("kernel_launches", C.c_longlong), ("launches_per_step", C.c_int),
                 ("passes_per_step", C.c_int), ("sweeps_per_pass", C.c_int), ("tile_rows", C.c_int),
                 ("pressure_iterations_last", C.c_int * 2), ("pressure_residual_last", C.c_double * 2),
-                ("nonfinite", C.c_int)]
+                ("nonfinite", C.c_int), ("learned_used", C.c_longlong), ("learned_fallback", C.c_longlong)]
 
 
 FS_NUM_KINDS = 5
@@ -95,6 +96,21 @@ SIGNATURES = {
     "fs_batch_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
     "fs_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "fs_autotune": (C.c_int, [C.POINTER(fs_config), _F, _F, _F, _I, C.c_char_p, C.POINTER(C.c_double)]),
+    "fs_conv_pack_weights": (C.c_int, [_P, _P, _P]),
+    "fs_conv3x3": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P]),
+    "fs_net_avgpool2": (C.c_int, [_P, _P, _I, _I, _P]),
+    "fs_net_avgpool2_bwd": (C.c_int, [_P, _P, _I, _I, _P]),
+    "fs_net_upsample2_bwd": (C.c_int, [_P, _P, _I, _I, _P]),
+    "fs_net_relu_bwd": (C.c_int, [_P, _P, _P, _P, _P, C.c_longlong, _I, _P]),
+    "fs_net_weight_grad": (C.c_int, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "fs_net_flip_weights": (C.c_int, [_P, _P, _P]),
+    "fs_net_mse": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P]),
+    "fs_net_adam": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _F, _F, _F, _F, _I, _P, _P]),
+    "fs_net_restrict": (C.c_int, [_P, _P, _I, _I, _I, _I, _F, _P, _P, _P, _P]),
+    "fs_net_prolong": (C.c_int, [_P, _P, _P, _I, _I, _I, _I, _P, _F, _P]),
+    "fs_set_network": (C.c_int, [_P, _P, C.c_longlong]),
+    "fs_capture_view": (C.c_int, [_P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "fs_memcpy_device": (C.c_int, [_P, _P, C.c_ulonglong, _P]),
     "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
     "fs_host_free": (C.c_int, [_P]),
     "fs_version": (C.c_char_p, []),
@@ -104,11 +120,13 @@ _lib = None
 
 
 def load(path: str | pathlib.Path | None = None):
-    """Load the CUDA library (raises if it has not been built)."""
+    """Load the CUDA library (raises if it has not been built). The FLUID2D_LIB
+    environment variable names an alternative build of the same library."""
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = pathlib.Path(path) if path else LIB_PATH
+    env = os.environ.get("FLUID2D_LIB")
+    p = pathlib.Path(path) if path else (pathlib.Path(env) if env else LIB_PATH)
     if not p.exists():
         raise RuntimeError(f"fluid2d_gb300: CUDA library not built ({p}); run build_lib.build()")
     L = C.CDLL(str(p))
@@ -231,7 +249,8 @@ class Solver:
                 "launches_per_step": st.launches_per_step, "passes_per_step": st.passes_per_step,
                 "sweeps_per_pass": st.sweeps_per_pass, "tile_rows": st.tile_rows,
                 "pressure_iterations_last": list(st.pressure_iterations_last),
-                "pressure_residual_last": list(st.pressure_residual_last), "nonfinite": st.nonfinite}
+                "pressure_residual_last": list(st.pressure_residual_last), "nonfinite": st.nonfinite,
+                "learned_used": st.learned_used, "learned_fallback": st.learned_fallback}
 
     def profile_step(self, diffusion_rate, viscosity, dt) -> dict:
         """One eager step with CUDA events around every launch; per kernel kind:
@@ -240,6 +259,15 @@ class Solver:
         _check(self._lib.fs_profile_step(self._h, diffusion_rate, viscosity, dt, C.byref(t)))
         return {KIND_NAMES[k]: {"launches": t.launches[k], "ms": t.ms[k], "bytes": t.algorithmic_bytes[k]}
                 for k in range(FS_NUM_KINDS)}
+
+    def set_network(self, params: np.ndarray):
+        params = np.ascontiguousarray(params, np.float32)
+        _check(self._lib.fs_set_network(self._h, params.ctypes.data, params.size))
+
+    def capture_view(self, slot: int):
+        d, p0, p1 = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _check(self._lib.fs_capture_view(self._h, slot, C.byref(d), C.byref(p0), C.byref(p1)))
+        return d.value, p0.value, p1.value
 
     def device_view(self) -> fs_device_view:
         v = fs_device_view()

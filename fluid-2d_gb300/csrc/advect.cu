@@ -145,11 +145,13 @@ __global__ void __launch_bounds__(256) advect_velocity_kernel(const float* __res
 // search. Persistent: the launch has a few waves' worth of CTAs that stride over all
 // blocks.
 
-__device__ __forceinline__ int find_job(const int* __restrict__ prefix, int n, int b) {
+constexpr int kSmemJobs = 2048;
+
+__device__ __forceinline__ int find_job(const int* __restrict__ sp, const int* __restrict__ prefix, int n, int b) {
     int lo = 0, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(prefix + mid) <= b) lo = mid;
+        if ((n <= kSmemJobs ? sp[mid] : __ldg(prefix + mid)) <= b) lo = mid;
         else hi = mid - 1;
     }
     return lo;
@@ -159,9 +161,14 @@ template <int OP>
 __global__ void __launch_bounds__(256) advect_batch_kernel(const AdvectJob* __restrict__ jobs,
                                                            const int* __restrict__ prefix, int njobs, int nblocks,
                                                            int* nonfinite) {
+    // the block prefix is searched in shared memory when it fits
+    __shared__ int sp[kSmemJobs];
+    if (njobs <= kSmemJobs)
+        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < njobs; i += blockDim.x * blockDim.y) sp[i] = prefix[i];
+    __syncthreads();
     int bad = 0;
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        const int g = find_job(prefix, njobs, b);
+        const int g = find_job(sp, prefix, njobs, b);
         const AdvectJob& J = jobs[g];
         const int lb = b - __ldg(prefix + g);
         const int bx = (J.A.cols + 31) / 32;

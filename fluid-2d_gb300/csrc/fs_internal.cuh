@@ -135,6 +135,14 @@ cudaError_t launch_splat(const float* d0, const float* u, const float* v, float*
                          cudaStream_t st);
 cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const AdvectArgs& A, int* nonfinite,
                                   cudaStream_t st);
+// Tensor-core conv set-up (shared-memory opt-in) on the current device (conv.cu).
+cudaError_t conv_prepare();
+
+// Learned warm start: residuals of the network's guess and of the previous pressure,
+// then keep the better one in `guess` (net.cu).
+cudaError_t launch_learned_select(const float* div, float* guess, const float* prev, int rows, int cols, int pitch,
+                                  double* res2, unsigned long long* counters, cudaStream_t st);
+
 int advect_batch_blocks(int rows, int cols);
 // op 0: splat, 1: density finish, 2: velocity backtrace; prefix[g] = first 32x8
 // block of job g (njobs + 1 entries, the last = nblocks).

@@ -27,6 +27,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "../../include/fluid2d_gb300.h"
 #include "fs_internal.cuh"
 
@@ -99,6 +101,23 @@ struct fs_solver {
     SolveCtrl* ctrl = nullptr;
     double* partials[2] = {};
     int solve_blocks = 0;
+    // training-data capture: each projection's divergence and starting pressure
+    float* cap_div[2] = {};
+    float* cap_start[2] = {};
+    // learned warm start (FS_WARM_LEARNED): network state on the FS_NET_GRID^2 grid
+    struct Net {
+        float* params = nullptr;          // FP32 [8][32*9*32 + 32]
+        __nv_bfloat16* wpk = nullptr;     // packed BF16 weights, 8 x 9216
+        __nv_bfloat16* act = nullptr;     // activations (see net_act)
+        float* y = nullptr;               // FP32 output, G*G*32
+        float* scale = nullptr;
+        int* err = nullptr;
+        unsigned long long* counters = nullptr;  // [guess used, fallback]
+        double* res = nullptr;            // two squared residuals
+        void* mem = nullptr;
+    } net;
+    float* pguess = nullptr;  // fine starting pressure built from the network
+    bool net_ready = false;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -252,6 +271,102 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
     return FS_OK;
 }
 
+constexpr int kNetG = FS_NET_GRID;
+constexpr int kNetC = 32;
+constexpr int kNetLayer = 32 * 9 * 32 + 32;
+constexpr float kNetKappa = kNetG * kNetG / 16.0f;
+// activation buffers (BF16, 32 channels): xin, e1, pool1, e2, e3, pool2, b1, b2, d1, d2, out
+constexpr int kNetActs = 11;
+inline size_t net_act_pixels(int k) {
+    const int lv[kNetActs] = {0, 0, 1, 1, 1, 2, 2, 2, 1, 0, 0};
+    const int g = kNetG >> lv[k];
+    return (size_t)g * g;
+}
+__nv_bfloat16* net_act(fs_solver* s, int k) {
+    size_t off = 0;
+    for (int i = 0; i < k; ++i) off += net_act_pixels(i) * kNetC;
+    return s->net.act + off;
+}
+
+// Starting pressure of one projection from the network: divergence-only pass,
+// restriction to the coarse grid, the 8-layer network on the tensor cores,
+// interpolation of its correction onto the previous pressure, and the residual
+// comparison that keeps the previous pressure when the guess is worse.
+int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, int slot, Counter& cnt) {
+    const float h = grid_h(s->rows, s->cols);
+    StencilLaunch L{};
+    L.nfields = 1;
+    StencilField& f = L.f[0];
+    set_geometry(f, s, 1);
+    f.s_lr = f.s_tb = 1.f;
+    f.kind = PASS_PRESSURE_FIRST;
+    f.sweeps = 0;
+    f.cdiv = -0.5f * h;
+    f.h = h;
+    f.x = u_in;
+    f.x2 = v_in;
+    f.cst_out = s->div;
+    CK(launch_stencil(L, s->tile_rows, s->stream));
+    cnt.launches++;
+    const float* prev = s->warm_valid ? s->pwarm[slot] : nullptr;
+    int rc = fs_net_restrict(s->div, prev, s->rows, s->cols, s->pitch, kNetG, kNetKappa, s->net.scale, net_act(s, 0),
+                             nullptr, s->stream);
+    if (rc != FS_OK) return rc;
+    cnt.launches += 2;
+    auto conv = [&](int li, int in, int out, int lvl, int up, int skip, int relu, float* yf) {
+        const int g = kNetG >> lvl;
+        return fs_conv3x3(net_act(s, in), s->net.wpk + (size_t)li * 9216, nullptr, s->net.params + (size_t)li * kNetLayer + 9216,
+                          skip >= 0 ? net_act(s, skip) : nullptr, out >= 0 ? net_act(s, out) : nullptr, yf, g, g, g, up,
+                          relu, 1, s->net.err, s->stream);
+    };
+    // e1 (G) -> pool -> e2, e3 (G/2) -> pool -> b1, b2 (G/4) -> d1 (+e3) -> d2 (+e1) -> out
+    if ((rc = conv(0, 0, 1, 0, 0, -1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = fs_net_avgpool2(net_act(s, 1), net_act(s, 2), kNetG / 2, kNetG / 2, s->stream)) != FS_OK) return rc;
+    if ((rc = conv(1, 2, 3, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = conv(2, 3, 4, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = fs_net_avgpool2(net_act(s, 4), net_act(s, 5), kNetG / 4, kNetG / 4, s->stream)) != FS_OK) return rc;
+    if ((rc = conv(3, 5, 6, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = conv(4, 6, 7, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = conv(5, 7, 8, 1, 1, 4, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = conv(6, 8, 9, 0, 1, 1, 1, nullptr)) != FS_OK) return rc;
+    if ((rc = conv(7, 9, 10, 0, 0, -1, 0, s->net.y)) != FS_OK) return rc;
+    cnt.launches += 10;
+    if ((rc = fs_net_prolong(s->net.y, prev, s->pguess, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa,
+                             s->stream)) != FS_OK)
+        return rc;
+    CK(launch_learned_select(s->div, s->pguess, prev, s->rows, s->cols, s->pitch, s->net.res, s->net.counters,
+                             s->stream));
+    cnt.launches += 3;
+    return FS_OK;
+}
+
+// Starting pressure of projection `slot`: the network's guess, the previous pressure,
+// or null (zero, as the reference), and its copy for training-data capture.
+int projection_start(fs_solver* s, const float* u_in, const float* v_in, int slot, Counter& cnt, const float** pin) {
+    const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
+    *pin = (warm && s->warm_valid) ? s->pwarm[slot] : nullptr;
+    if (s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready) {
+        int rc = enqueue_learned_guess(s, u_in, v_in, slot, cnt);
+        if (rc != FS_OK) return rc;
+        *pin = s->pguess;
+    }
+    if (s->cfg.capture) {
+        if (*pin)
+            CK(cudaMemcpyAsync(s->cap_start[slot], *pin, s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                               s->stream));
+        else
+            CK(cudaMemsetAsync(s->cap_start[slot], 0, s->field_floats * sizeof(float), s->stream));
+    }
+    return FS_OK;
+}
+
+int capture_div(fs_solver* s, int slot) {
+    if (!s->cfg.capture) return FS_OK;
+    CK(cudaMemcpyAsync(s->cap_div[slot], s->div, s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                       s->stream));
+    return FS_OK;
+}
+
 // project (fluid_solver_gpu.cu:358-404): (u_in, v_in) -> (u_out, v_out). slot picks
 // the warm-start pressure buffer (the two projections of a step keep separate ones).
 // Residual-driven projection: one persistent cooperative launch runs depth-K passes
@@ -259,7 +374,7 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
 // iteration cap is reached, then the gradient subtract (see pressure_solve_kernel).
 int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
                                 int slot, Counter& cnt) {
-    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
     const int K = s->sweeps;
     PressureSolve P{};
@@ -270,10 +385,13 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
         f->cdiv = -0.5f * h;
         f->h = h;
     }
+    const float* pin = nullptr;
+    int rc = projection_start(s, u_in, v_in, slot, cnt, &pin);
+    if (rc != FS_OK) return rc;
     P.first.kind = PASS_PRESSURE_FIRST;
     P.first.x = u_in;
     P.first.x2 = v_in;
-    P.first.cst = (warm && s->warm_valid) ? s->pwarm[slot] : nullptr;
+    P.first.cst = pin;
     P.first.cst_out = s->div;
     P.mid.kind = PASS_PRESSURE;
     P.mid.cst = s->div;
@@ -304,7 +422,7 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
     PROF_END(s, FS_KIND_STENCIL, 0.0);  // bytes depend on the iteration count reached
     cnt.launches++;
     cnt.passes++;
-    return FS_OK;
+    return capture_div(s, slot);
 }
 
 int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out, int slot,
@@ -312,9 +430,11 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
     if (s->cfg.pressure_tolerance > 0.f) return enqueue_project_to_residual(s, u_in, v_in, u_out, v_out, slot, cnt);
     const std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
     const int m = (int)plan.size();
-    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
-    const float* pin = (warm && s->warm_valid) ? s->pwarm[slot] : nullptr;
+    const float* pin = nullptr;
+    int rc = projection_start(s, u_in, v_in, slot, cnt, &pin);
+    if (rc != FS_OK) return rc;
     for (int pass = 0; pass < m; ++pass) {
         const bool last = pass == m - 1;
         StencilLaunch L{};
@@ -355,6 +475,7 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
         PROF_END(s, FS_KIND_STENCIL, bytes);
         cnt.launches++;
         cnt.passes++;
+        if (pass == 0 && (rc = capture_div(s, slot)) != FS_OK) return rc;
     }
     if (warm && m == 1) {
         CK(cudaMemcpyAsync(s->pwarm[slot], s->p[0], s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,
@@ -409,7 +530,7 @@ void destroy_graph(fs_solver* s) {
 
 int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
     int rc;
-    const bool warm = s->cfg.warm_start == FS_WARM_PREVIOUS;
+    const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     for (int k = 0; k < nsteps; ++k) {
         // The first warm-start step starts from zero pressure; its graph differs.
         bool graphable = s->cfg.use_graph && (!warm || s->warm_valid);
@@ -542,8 +663,10 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     if ((long long)cfg->rows * cfg->cols > (1LL << 31)) return fail(FS_ERR_ARG, "fs_create: grid too large");
     if (cfg->diffuse_iterations < 0 || cfg->pressure_iterations < 0)
         return fail(FS_ERR_ARG, "fs_create: negative iteration count");
-    if (cfg->warm_start != FS_WARM_ZERO && cfg->warm_start != FS_WARM_PREVIOUS)
+    if (cfg->warm_start != FS_WARM_ZERO && cfg->warm_start != FS_WARM_PREVIOUS && cfg->warm_start != FS_WARM_LEARNED)
         return fail(FS_ERR_ARG, "fs_create: unknown warm_start mode");
+    if (cfg->warm_start == FS_WARM_LEARNED && (cfg->rows != cfg->cols || (cfg->rows - 2) % FS_NET_GRID != 0))
+        return fail(FS_ERR_ARG, "fs_create: the learned warm start needs a square grid with interior % 32 == 0");
     if (cfg->tile_rows != 0 && cfg->tile_rows != 64 && cfg->tile_rows != 128)
         return fail(FS_ERR_ARG, "fs_create: tile_rows must be 0, 64 or 128");
     if (cfg->pressure_tolerance < 0.f || cfg->pressure_tolerance != cfg->pressure_tolerance)
@@ -576,7 +699,8 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         delete s;
         return cuda_fail(e, "fs_create: stencil kernel set-up");
     }
-    const int nfields = 6 + 9 + 6 + 2;
+    const bool learned = cfg->warm_start == FS_WARM_LEARNED;
+    const int nfields = 6 + 9 + 6 + 2 + (cfg->capture ? 4 : 0) + (learned ? 1 : 0);
     // tail: flags (256 B), two solve control blocks, two partial-sum arrays
     const size_t part_doubles = 4 * (size_t)std::max(1, s->solve_blocks);
     const size_t tail = 256 + 2 * 256 + 2 * part_doubles * sizeof(double);
@@ -607,6 +731,13 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     s->vel1[1] = take();
     s->pwarm[0] = take();
     s->pwarm[1] = take();
+    if (cfg->capture) {
+        for (int k = 0; k < 2; ++k) {
+            s->cap_div[k] = take();
+            s->cap_start[k] = take();
+        }
+    }
+    if (learned) s->pguess = take();
     char* tailp = reinterpret_cast<char*>(p);
     s->flags = reinterpret_cast<int*>(tailp);
     s->ctrl = reinterpret_cast<SolveCtrl*>(tailp + 256);
@@ -617,7 +748,31 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         rc = cuda_fail(e, "fs_create: cudaMemset");
     else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaStreamCreate");
+    if (rc == FS_OK && learned) {
+        size_t acts = 0;
+        for (int k = 0; k < kNetActs; ++k) acts += net_act_pixels(k) * kNetC;
+        const size_t bytes = (size_t)FS_NET_PARAMS * 4 + 8 * 9216 * 2 + acts * 2 + (size_t)kNetG * kNetG * kNetC * 4 +
+                             256 * 4;
+        if ((e = cudaMalloc(&s->net.mem, bytes)) != cudaSuccess || (e = cudaMemset(s->net.mem, 0, bytes)) != cudaSuccess) {
+            rc = cuda_fail(e, "fs_create: network buffers");
+        } else {
+            char* q = static_cast<char*>(s->net.mem);
+            s->net.params = reinterpret_cast<float*>(q);
+            q += (size_t)FS_NET_PARAMS * 4;
+            s->net.wpk = reinterpret_cast<__nv_bfloat16*>(q);
+            q += 8 * 9216 * 2;
+            s->net.act = reinterpret_cast<__nv_bfloat16*>(q);
+            q += acts * 2;
+            s->net.y = reinterpret_cast<float*>(q);
+            q += (size_t)kNetG * kNetG * kNetC * 4;
+            s->net.res = reinterpret_cast<double*>(q);
+            s->net.counters = reinterpret_cast<unsigned long long*>(q + 16);
+            s->net.scale = reinterpret_cast<float*>(q + 32);
+            s->net.err = reinterpret_cast<int*>(q + 36);
+        }
+    }
     if (rc != FS_OK) {
+        if (s->net.mem) cudaFree(s->net.mem);
         if (s->stream) cudaStreamDestroy(s->stream);
         cudaFree(s->slab);
         delete s;
@@ -635,6 +790,7 @@ int fs_destroy(fs_solver* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     destroy_graph(s);
     if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->net.mem) cudaFree(s->net.mem);
     cudaFree(s->slab);
     delete s;
     return FS_OK;
@@ -776,6 +932,39 @@ int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float d
     return rc;
 }
 
+int fs_set_network(fs_solver* s, const float* params, long long count) {
+    if (!s || !params) return fail(FS_ERR_ARG, "fs_set_network: null argument");
+    if (count != FS_NET_PARAMS) return fail(FS_ERR_ARG, "fs_set_network: expected FS_NET_PARAMS parameters");
+    if (s->cfg.warm_start != FS_WARM_LEARNED || !s->net.mem)
+        return fail(FS_ERR_STATE, "fs_set_network: the handle was not created with FS_WARM_LEARNED");
+    DeviceGuard g(s->device);
+    CK(conv_prepare());
+    CK(cudaMemcpyAsync(s->net.params, params, (size_t)count * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    for (int li = 0; li < 8; ++li) {
+        int rc = fs_conv_pack_weights(s->net.params + (size_t)li * kNetLayer, s->net.wpk + (size_t)li * 9216, s->stream);
+        if (rc != FS_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->net_ready = true;
+    destroy_graph(s);  // the step plan changes
+    return FS_OK;
+}
+
+int fs_capture_view(fs_solver* s, int slot, float** div, float** p_start, float** p_final) {
+    if (!s || slot < 0 || slot > 1) return fail(FS_ERR_ARG, "fs_capture_view: bad argument");
+    if (div) *div = s->cap_div[slot];
+    if (p_start) *p_start = s->cap_start[slot];
+    if (p_final) *p_final = s->cfg.warm_start != FS_WARM_ZERO ? s->pwarm[slot] : nullptr;
+    if (!s->cfg.capture) return fail(FS_ERR_STATE, "fs_capture_view: the handle was created without capture");
+    return FS_OK;
+}
+
+int fs_memcpy_device(void* dst, const void* src, unsigned long long bytes, void* stream) {
+    if (!dst || !src) return fail(FS_ERR_ARG, "fs_memcpy_device: null pointer");
+    CK(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return FS_OK;
+}
+
 int fs_get_stats(const fs_solver* s, fs_stats* out) {
     if (!s || !out) return fail(FS_ERR_ARG, "fs_get_stats: null argument");
     *out = s->stats;
@@ -784,6 +973,14 @@ int fs_get_stats(const fs_solver* s, fs_stats* out) {
     out->sweeps_per_pass = s->sweeps;
     out->tile_rows = s->tile_rows;
     out->pressure_iterations_last[0] = out->pressure_iterations_last[1] = s->cfg.pressure_iterations;
+    if (s->net_ready) {
+        DeviceGuard g(s->device);
+        unsigned long long c[2] = {0, 0};
+        CK(cudaMemcpyAsync(c, s->net.counters, sizeof(c), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        out->learned_used = (long long)c[0];
+        out->learned_fallback = (long long)c[1];
+    }
     if (s->cfg.pressure_tolerance > 0.f && s->stats.steps > 0) {
         DeviceGuard g(s->device);
         SolveCtrl c[2];

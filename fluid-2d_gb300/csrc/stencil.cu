@@ -55,73 +55,69 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
     return __fmul_rn(s, 0.25f);
 }
 
-// All sweeps of one tile. Each thread owns one column of SR rows: its values and its
-// constant term (x0 or div) live in registers; horizontal neighbours and the rows just
-// above/below the strip come from `cur` (the previous sweep), new values go to
-// registers and `nxt`, one barrier per sweep.
+// All sweeps of one tile. Each thread owns one column of SR rows of the region and
+// keeps only its constant term (x0 or div) in registers: every sweep streams down the
+// column with a rolling up/centre/down window read from `cur` (the previous sweep) plus
+// the left and right neighbours, and writes the new value to `nxt` — three shared loads
+// and one store per cell update, and no per-row state carried across sweeps. One
+// barrier per sweep.
 //   EDGE = false: the region lies inside the domain interior; every cell updates, no
 //                 checks (cells near the region border compute values that nothing
 //                 stored depends on).
-//   EDGE = true:  bit i of `live` marks interior cells; after each sweep the domain-edge
-//                 cells take their inner neighbour's new value (set_boundary_*,
-//                 fluid_solver_gpu.cu:11-54): etop/ebot mark top/bottom edge cells,
-//                 eside left/right edge cells (neighbour column side_src); corners keep
-//                 their value.
+//   EDGE = true:  bit i of `live` marks interior cells (others keep their value); after
+//                 each sweep the domain-edge cells take their inner neighbour's new value
+//                 (set_boundary_*, fluid_solver_gpu.cu:11-54); corners keep theirs.
 template <bool DIFF, bool EDGE, int SR, int RH>
-__device__ __forceinline__ void run_sweeps(float (&c)[SR], const float (&k)[SR], float*& cur, float*& nxt,
-                                           int nsweeps, int r0, int tx, int txl, int txr, unsigned live, int gy0,
-                                           int gc, int rows, int cols, float s_lr, float s_tb, float a, float dh,
-                                           float dl, float rf) {
+__device__ __forceinline__ void run_sweeps(const float (&k)[SR], int& co, int& no, int nsweeps, int r0,
+                                           int tx, int txl, int txr, unsigned live, int gy0, int gc, int rows,
+                                           int cols, float s_lr, float s_tb, float a, float dh, float dl,
+                                           float rf) {
     constexpr int RW = kRegionW;
+    extern __shared__ float4 smem4[];
+    float* const S = reinterpret_cast<float*>(smem4);
+    const int rup = r0 > 0 ? r0 - 1 : 0;
+    const int rlast = (r0 + SR < RH) ? r0 + SR : r0 + SR - 1;
 #pragma unroll 1
     for (int s = 0; s < nsweeps; ++s) {
-        const float* __restrict__ cr = cur;
-        float* __restrict__ nx = nxt;
-        float up = (r0 > 0) ? cr[(r0 - 1) * RW + tx] : c[0];
-        const float dn = (r0 + SR < RH) ? cr[(r0 + SR) * RW + tx] : c[SR - 1];
+        const float* __restrict__ cr = S + co;
+        float* __restrict__ nx = S + no;
+        float up = cr[rup * RW + tx];
+        float ce = cr[r0 * RW + tx];
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const float old = c[i];
-            const float down = (i + 1 < SR) ? c[i + 1] : dn;
-            const float Lv = cr[(r0 + i) * RW + txl], Rv = cr[(r0 + i) * RW + txr];
-            float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, down, a, dh, dl, rf)
-                            : pressure_update(k[i], Lv, Rv, up, down);
-            if (EDGE) nv = ((live >> i) & 1u) ? nv : old;
-            c[i] = nv;
-            nx[(r0 + i) * RW + tx] = nv;
-            up = old;
+            const int r = r0 + i;
+            const float dn = cr[(i + 1 < SR ? r + 1 : rlast) * RW + tx];
+            const float Lv = cr[r * RW + txl], Rv = cr[r * RW + txr];
+            float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, dn, a, dh, dl, rf)
+                            : pressure_update(k[i], Lv, Rv, up, dn);
+            if (EDGE) nv = ((live >> i) & 1u) ? nv : ce;
+            nx[r * RW + tx] = nv;
+            up = ce;
+            ce = dn;
         }
         __syncthreads();
         if (EDGE) {
             const bool col_int = gc >= 1 && gc <= cols - 2;
-#pragma unroll
             for (int i = 0; i < SR; ++i) {
                 const int r = r0 + i, gr = gy0 + r;
-                float val;
+                int src = -1;
+                float sg = 1.f;
                 if (col_int) {
-                    if (gr == 0)
-                        val = s_tb * nx[min(r + 1, RH - 1) * RW + tx];
-                    else if (gr == rows - 1)
-                        val = s_tb * nx[max(r - 1, 0) * RW + tx];
-                    else
-                        continue;
+                    if (gr == 0) src = min(r + 1, RH - 1) * RW + tx;
+                    else if (gr == rows - 1) src = max(r - 1, 0) * RW + tx;
+                    sg = s_tb;
                 } else if (gr >= 1 && gr <= rows - 2) {
-                    if (gc == 0)
-                        val = s_lr * nx[r * RW + txr];
-                    else if (gc == cols - 1)
-                        val = s_lr * nx[r * RW + txl];
-                    else
-                        continue;
-                } else {
-                    continue;
+                    if (gc == 0) src = r * RW + txr;
+                    else if (gc == cols - 1) src = r * RW + txl;
+                    sg = s_lr;
                 }
-                c[i] = val;
-                nx[r * RW + tx] = val;
+                if (src >= 0) nx[r * RW + tx] = sg * nx[src];
             }
             __syncthreads();
         }
-        cur = nx;
-        nxt = const_cast<float*>(cr);
+        const int t = co;
+        co = no;
+        no = t;
     }
 }
 
@@ -132,9 +128,12 @@ __device__ __forceinline__ void run_sweeps(float (&c)[SR], const float (&k)[SR],
 // a persistent caller can ping-pong buffers across passes.
 template <int TY, int SR, bool DIFF>
 __device__ __forceinline__ void process_tile(const StencilField& F, int b, const float* __restrict__ xin,
-                                             float* __restrict__ yout, float* cur, float* nxt, bool resid,
+                                             float* __restrict__ yout, bool resid,
                                              float& rnum, float& rden) {
     constexpr int RW = kRegionW, RH = TY * SR;
+    extern __shared__ float4 smem4[];
+    float* const S = reinterpret_cast<float*>(smem4);
+    int co = 0, no = RH * RW;  // offsets of the current / next sweep buffers in S
     __syncthreads();  // the previous tile of this CTA may still be reading shared memory
     const int tyi = b / F.tiles_x, txi = b - tyi * F.tiles_x;
     const int H = F.halo;
@@ -161,8 +160,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             const int gr = gy0 + r0 + i;
             const bool in = col_in && gr >= 0 && gr < rows;
             const size_t o = (size_t)gr * pitch + gc;
-            cur[(r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
-            nxt[(r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
+            S[co + (r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
+            S[no + (r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
         }
         __syncthreads();
         const float cdiv = F.cdiv;
@@ -170,9 +169,9 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         for (int i = 0; i < SR; ++i) {
             const int r = r0 + i, gr = gy0 + r;
             const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
-            float s = __fsub_rn(cur[r * RW + txr], cur[r * RW + txl]);
-            s = __fadd_rn(s, nxt[rd * RW + tx]);
-            s = __fsub_rn(s, nxt[ru * RW + tx]);
+            float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
+            s = __fadd_rn(s, S[no + rd * RW + tx]);
+            s = __fsub_rn(s, S[no + ru * RW + tx]);
             const bool interior = col_int && gr >= 1 && gr <= rows - 2;
             k[i] = interior ? __fmul_rn(cdiv, s) : 0.f;
             const bool in = col_in && gr >= 0 && gr < rows;
@@ -205,7 +204,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         }
     }
 #pragma unroll
-    for (int i = 0; i < SR; ++i) cur[(r0 + i) * RW + tx] = c[i];
+    for (int i = 0; i < SR; ++i) S[co + (r0 + i) * RW + tx] = c[i];
     __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
@@ -217,12 +216,15 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             const int gr = gy0 + r0 + i;
             live |= (unsigned)(col_int && gr >= 1 && gr <= rows - 2) << i;
         }
-        run_sweeps<DIFF, true, SR, RH>(c, k, cur, nxt, F.sweeps, r0, tx, txl, txr, live, gy0, gc, rows, cols,
-                                       F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf);
+        run_sweeps<DIFF, true, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, live, gy0, gc, rows, cols, F.s_lr,
+                                       F.s_tb, F.a, F.dh, F.dl, F.rf);
     } else {
-        run_sweeps<DIFF, false, SR, RH>(c, k, cur, nxt, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
+        run_sweeps<DIFF, false, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
                                         F.s_tb, F.a, F.dh, F.dl, F.rf);
     }
+    // final values of this thread's column (S + co is complete after the last barrier)
+#pragma unroll
+    for (int i = 0; i < SR; ++i) c[i] = S[co + (r0 + i) * RW + tx];
 
     // ------------------------------------------------------------------ store
     const bool col_out = col_in && tx >= H && tx < H + F.tile_w;
@@ -272,8 +274,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
                 const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
                 const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
                 const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
-                const float gu = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rr * RW + rcr], cur[rr * RW + rcl])), h);
-                const float gv = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(cur[rrd * RW + rc], cur[rru * RW + rc])), h);
+                const float gu = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rr * RW + rcr], S[co + rr * RW + rcl])), h);
+                const float gv = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rrd * RW + rc], S[co + rru * RW + rc])), h);
                 const size_t oi = (size_t)ir * pitch + ic;
                 un = su * __fsub_rn(__ldcg(F.u_in + oi), gu);
                 vn = sv * __fsub_rn(__ldcg(F.v_in + oi), gv);
@@ -294,10 +296,10 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             const int r = r0 + i, gr = gy0 + r;
             if (r < H || r >= H + F.tile_h || !col_int || gr < 1 || gr > rows - 2) continue;
             const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
-            float sres = k[i] + cur[r * RW + txr];
-            sres += cur[r * RW + txl];
-            sres += cur[rd * RW + tx];
-            sres += cur[ru * RW + tx];
+            float sres = k[i] + S[co + r * RW + txr];
+            sres += S[co + r * RW + txl];
+            sres += S[co + rd * RW + tx];
+            sres += S[co + ru * RW + tx];
             const float res = sres - 4.f * c[i];
             rnum = fmaf(res, res, rnum);
             rden = fmaf(k[i], k[i], rden);
@@ -311,14 +313,12 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     stencil_kernel(const __grid_constant__ StencilLaunch L) {
     constexpr int RH = TY * SR;
     extern __shared__ float4 smem4[];
-    float* cur = reinterpret_cast<float*>(smem4);
-    float* nxt = cur + RH * kRegionW;
     int b = blockIdx.x, f = 0;
 #pragma unroll 1
     while (f + 1 < L.nfields && b >= L.f[f + 1].tile_begin) ++f;
     const StencilField& F = L.f[f];
     float rn = 0.f, rd = 0.f;
-    process_tile<TY, SR, DIFF>(F, b - F.tile_begin, F.x, F.y, cur, nxt, false, rn, rd);
+    process_tile<TY, SR, DIFF>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
 }
 
 // One pass over a device-resident table of fields (a batch of grids of uneven
@@ -328,21 +328,31 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
 template <int TY, int SR, bool DIFF>
 __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     stencil_table_kernel(const StencilField* __restrict__ tab, const int* __restrict__ prefix, int nf, int total) {
-    constexpr int RH = TY * SR;
-    extern __shared__ float4 smem4[];
-    float* cur = reinterpret_cast<float*>(smem4);
-    float* nxt = cur + RH * kRegionW;
+    // the tile prefix of up to kSmemPrefix fields is searched in shared memory
+    constexpr int kSmemPrefix = 2048;
+    __shared__ int sp[kSmemPrefix];
+    const bool in_smem = nf <= kSmemPrefix;
+    if (in_smem)
+        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nf; i += blockDim.x * blockDim.y) sp[i] = prefix[i];
+    __syncthreads();
 #pragma unroll 1
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         int lo = 0, hi = nf - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(prefix + mid) <= t) lo = mid;
+            if ((in_smem ? sp[mid] : __ldg(prefix + mid)) <= t) lo = mid;
             else hi = mid - 1;
         }
-        const StencilField& F = tab[lo];
+        // stage this grid's descriptor in shared memory (read many times per tile)
+        __shared__ StencilField sF;
+        static_assert(sizeof(StencilField) % 4 == 0, "descriptor copied as words");
+        __syncthreads();
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+        if (tid < (int)(sizeof(StencilField) / 4))
+            reinterpret_cast<int*>(&sF)[tid] = __ldg(reinterpret_cast<const int*>(tab + lo) + tid);
+        __syncthreads();
         float rn = 0.f, rd = 0.f;
-        process_tile<TY, SR, DIFF>(F, t - __ldg(prefix + lo), F.x, F.y, cur, nxt, false, rn, rd);
+        process_tile<TY, SR, DIFF>(sF, t - __ldg(prefix + lo), sF.x, sF.y, false, rn, rd);
     }
 }
 
@@ -418,18 +428,14 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 // Out-of-line tile call for the persistent kernel: keeps the pass loop's state out
 // of the tile body's register budget.
 template <int TY, int SR>
-__device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, float* cur,
-                                           float* nxt, bool resid, float& rn, float& rd) {
-    process_tile<TY, SR, false>(F, t, x, y, cur, nxt, resid, rn, rd);
+__device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, bool resid,
+                                           float& rn, float& rd) {
+    process_tile<TY, SR, false>(F, t, x, y, resid, rn, rd);
 }
 
 template <int TY, int SR>
 __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     pressure_solve_kernel(const __grid_constant__ PressureSolve P) {
-    constexpr int RH = TY * SR;
-    extern __shared__ float4 smem4[];
-    float* cur = reinterpret_cast<float*>(smem4);
-    float* nxt = cur + RH * kRegionW;
     const unsigned G = gridDim.x;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
     const int ntiles = P.mid.tiles_x * P.mid.tiles_y;
@@ -443,7 +449,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
         float rn = 0.f, rd = 0.f;
 #pragma unroll 1
         for (int t = blockIdx.x; t < ntiles; t += G)
-            pressure_tile<TY, SR>(F, t, x, P.p[pass & 1], cur, nxt, true, rn, rd);
+            pressure_tile<TY, SR>(F, t, x, P.p[pass & 1], true, rn, rd);
         double a = rn, b = rd;
         block_sum2(a, b);
         double* part = P.partials + (size_t)(pass & 1) * 2 * G;
@@ -472,7 +478,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
         float rn = 0.f, rd = 0.f;
 #pragma unroll 1
         for (int t = blockIdx.x; t < nfin; t += G)
-            pressure_tile<TY, SR>(P.fin, t, pf, P.p_out, cur, nxt, false, rn, rd);
+            pressure_tile<TY, SR>(P.fin, t, pf, P.p_out, false, rn, rd);
     }
     if (blockIdx.x == 0 && tid == 0) {
         P.ctrl->passes = passes;

@@ -1,0 +1,159 @@
+"""Training data and training loop for the learned pressure warm start.
+
+Data: seeded random-vortex runs of the solver itself (previous-pressure warm start,
+capture on). For every projection the solver keeps the divergence it projected and the
+pressure it started from; the exact solution p* of the same discrete Neumann problem
+(4p - sum of neighbours = div on the interior, edges equal to their inner neighbour) is
+computed in FP64 with the discrete cosine transform that diagonalises it, and the
+training target is the block-mean correction p*_c - p_start_c on the coarse grid, zero
+mean, in network units. Inputs come from the same restriction kernel the solver runs at
+inference (fs_net_restrict), so training and inference see identical preprocessing.
+
+Training: Adam on mean squared error, forward and backward on the project's kernels
+(learned.Net). torch supplies device buffers and the FP64 DCT matrices only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+
+from . import learned as Lm
+
+G = Lm.G
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def dct_basis(n, device):
+    """Orthonormal DCT-II matrix C (C @ x transforms along the first axis) and the
+    eigenvalues 2 - 2cos(pi k / n) of the 1-D reflective-Neumann second difference."""
+    torch = _torch()
+    k = torch.arange(n, dtype=torch.float64, device=device)[:, None]
+    i = torch.arange(n, dtype=torch.float64, device=device)[None, :]
+    Cm = torch.cos(math.pi * k * (2 * i + 1) / (2 * n)) * math.sqrt(2.0 / n)
+    Cm[0] /= math.sqrt(2.0)
+    lam = 2.0 - 2.0 * torch.cos(math.pi * torch.arange(n, dtype=torch.float64, device=device) / n)
+    return Cm, lam
+
+
+def neumann_solve(div, Cm, lam):
+    """Exact zero-mean solution of 4p - sum(nbrs) = div on an n x n interior with
+    reflective edges (the fixed point of the reference's Jacobi iteration)."""
+    torch = _torch()
+    dh = Cm @ div @ Cm.T
+    den = lam[:, None] + lam[None, :]
+    den[0, 0] = 1.0
+    ph = dh / den
+    ph[0, 0] = 0.0
+    return Cm.T @ ph @ Cm
+
+
+def _view(ptr, rows, pitch, device):
+    """Copy a pitched device field (rows x pitch floats at ptr) into a torch tensor."""
+    torch = _torch()
+    from . import load
+
+    out = torch.empty((rows, pitch), dtype=torch.float32, device=device)
+    rc = load().fs_memcpy_device(C.c_void_p(out.data_ptr()), C.c_void_p(ptr), rows * pitch * 4, None)
+    if rc != 0:
+        raise RuntimeError("fs_memcpy_device failed")
+    return out
+
+
+def generate(n_samples, size=512, steps_per_run=100, seed=100, kp=40, device="cuda", log=None):
+    """Returns (X [S, G, G, 32] BF16 network inputs, T [S, G, G] FP32 targets, info)."""
+    torch = _torch()
+    import fluid2d_gb300 as pkg
+    from fluid2d_gb300 import workloads
+
+    L = pkg.load()
+    Cm, lam = dct_basis(size, device)
+    R = size // G
+    xs, ts = [], []
+    scale = torch.zeros(1, dtype=torch.float32, device=device)
+    run = 0
+    t0 = time.time()
+    while len(ts) < n_samples:
+        w = workloads.vortex_field(size, seed=seed + run, kd=20, kp=kp, dt=0.05, rate=1e-5, vortices=16,
+                                   rmin=size / 100.0, rmax=size / 25.0)
+        s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=kp, warm_start=pkg.FS_WARM_PREVIOUS,
+                       capture=1, check_finite=0, device=0)
+        s.upload(*w.state())
+        s.upload_sources(*w.sources())
+        pitch = s.device_view().pitch
+        for _ in range(steps_per_run):
+            s.step(w.diffusion, w.viscosity, w.dt, 1)
+            for slot in (0, 1):
+                dptr, sptr, _ = s.capture_view(slot)
+                xin = torch.zeros((G, G, 32), dtype=torch.bfloat16, device=device)
+                pc = torch.zeros((G, G), dtype=torch.float32, device=device)
+                rc = L.fs_net_restrict(C.c_void_p(dptr), C.c_void_p(sptr), w.rows, w.cols, pitch, G, Lm.KAPPA,
+                                       C.c_void_p(scale.data_ptr()), C.c_void_p(xin.data_ptr()),
+                                       C.c_void_p(pc.data_ptr()), None)
+                if rc != 0:
+                    raise RuntimeError(L.fs_last_error().decode())
+                div = _view(dptr, w.rows, pitch, device)[1:-1, 1:size + 1].double()
+                pstar = neumann_solve(div, Cm, lam)
+                pstar_c = pstar.reshape(G, R, G, R).mean(dim=(1, 3)).float()
+                corr = pstar_c - pc
+                corr = corr - corr.mean()
+                xs.append(xin)
+                ts.append(corr / (scale * Lm.KAPPA))
+                if len(ts) >= n_samples:
+                    break
+            if len(ts) >= n_samples:
+                break
+        s.close()
+        run += 1
+        if log:
+            log(f"generated {len(ts)} samples ({run} runs, {time.time() - t0:.1f} s)")
+    X = torch.stack(xs)
+    T = torch.stack(ts)
+    return X, T, {"runs": run, "size": size, "seconds": time.time() - t0}
+
+
+def train(X, T, epochs=4, batch=128, lr=1e-3, seed=0, log=None):
+    """Trains the network on (X, T); returns (params as numpy, loss history)."""
+    torch = _torch()
+    dev = X.device
+    S = X.shape[0]
+    params = torch.from_numpy(Lm.init_params(seed)).to(dev)
+    net = Lm.Net(B=batch, params=params)
+    opt = Lm.Adam(net, lr=lr)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    hist = []
+    for ep in range(epochs):
+        perm = torch.randperm(S, generator=g)
+        for b0 in range(0, S - batch + 1, batch):
+            idx = perm[b0:b0 + batch].to(dev)
+            x0 = X[idx].reshape(batch * G, G, 32).contiguous()
+            t = T[idx].reshape(batch * G, G).contiguous()
+            net.forward(x0)
+            loss, dy = Lm.mse_loss(net, t)
+            grad = net.backward(x0, dy)
+            opt.step(grad)
+            hist.append(float(loss))
+        if log:
+            log(f"epoch {ep}: loss {np.mean(hist[-max(1, S // batch):]):.4e}")
+    return params.cpu().numpy(), hist
+
+
+def evaluate_loss(params, X, T, batch=128):
+    torch = _torch()
+    net = Lm.Net(B=batch, params=torch.from_numpy(np.asarray(params, np.float32)).to(X.device))
+    tot, n = 0.0, 0
+    for b0 in range(0, X.shape[0] - batch + 1, batch):
+        x0 = X[b0:b0 + batch].reshape(batch * G, G, 32).contiguous()
+        t = T[b0:b0 + batch].reshape(batch * G, G).contiguous()
+        net.forward(x0)
+        loss, _ = Lm.mse_loss(net, t)
+        tot += float(loss)
+        n += 1
+    return tot / max(n, 1)

@@ -50,6 +50,7 @@ extern "C" {
  * p_buffer.clear(0), src/fluid_solver_gpu.cu:364). */
 #define FS_WARM_ZERO 0
 #define FS_WARM_PREVIOUS 1
+#define FS_WARM_LEARNED 2 /* network correction of the previous pressure (fs_set_network) */
 
 typedef struct fs_solver fs_solver;
 
@@ -67,6 +68,8 @@ typedef struct fs_config {
     float pressure_tolerance;  /* > 0: run the pressure solve to this relative residual */
     int pressure_max_iterations; /* iteration cap when pressure_tolerance > 0 */
     int check_finite;          /* 1: flag NaN/Inf in the step's outputs (FS_ERR_NONFINITE) */
+    int capture;               /* 1: keep each projection's divergence and starting pressure
+                                  for fs_capture_view (training-data generation) */
 } fs_config;
 
 typedef struct fs_stats {
@@ -79,6 +82,8 @@ typedef struct fs_stats {
     int pressure_iterations_last[2]; /* sweeps used by the two projections of the last step */
     double pressure_residual_last[2];/* their final relative residuals (residual mode only) */
     int nonfinite;                   /* 1 if a NaN/Inf was flagged since the last check */
+    long long learned_used;          /* projections that started from the network's guess */
+    long long learned_fallback;      /* projections that kept the previous pressure instead */
 } fs_stats;
 
 /* Device view of the resident state, for zero-copy use by other CUDA code. Each field
@@ -126,6 +131,24 @@ FS_API int fs_sync(fs_solver* s);
 
 FS_API int fs_get_stats(const fs_solver* s, fs_stats* out);
 FS_API int fs_device_view_get(fs_solver* s, fs_device_view* out);
+
+/* Learned warm start (FS_WARM_LEARNED): load the network's FP32 parameters (8 layers x
+ * (32x9x32 weights [co][tap][ci] + 32 biases) = FS_NET_PARAMS floats, host memory). The
+ * grid must be square with an interior divisible by FS_NET_GRID. Each projection then
+ * computes the divergence, runs the network on the FS_NET_GRID^2 coarse grid, adds the
+ * interpolated correction to the previous pressure, and starts Jacobi from whichever of
+ * that guess and the previous pressure has the smaller residual. */
+#define FS_NET_GRID 32
+#define FS_NET_PARAMS (8 * (32 * 9 * 32 + 32))
+FS_API int fs_set_network(fs_solver* s, const float* params, long long count);
+
+/* Device pointers (rows x pitch, see fs_device_view) to the divergence and the starting
+ * pressure of projection `slot` (0 or 1) of the last step, and to its final pressure;
+ * requires cfg.capture (divergence, start) and a warm-start mode (final). */
+FS_API int fs_capture_view(fs_solver* s, int slot, float** div, float** p_start, float** p_final);
+
+/* Device-to-device copy on a stream (helper for callers holding raw device pointers). */
+FS_API int fs_memcpy_device(void* dst, const void* src, unsigned long long bytes, void* stream);
 
 /* Single stages of the step on the resident state, for kernel-level checks. The
  * stage runs with the handle's sweep counts and leaves its result in the state. */
@@ -203,6 +226,44 @@ FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, 
 #define FS_NOALLOC_MAX_CELLS 1048576
 FS_API int fs_project_noalloc(const float* u, const float* v, float* u_out, float* v_out, int rows, int cols,
                               int pitch, int iterations, void* stream);
+
+/* 3x3 convolution building block of the learned pressure warm start (no counterpart
+ * in the reference). Activations are NHWC BF16 with 32 channels; output (H x W), input
+ * (H x W) or (H/2 x W/2) nearest-upsampled when up = 1; zero padding. y = act(conv(x) +
+ * bias + skip), act = ReLU when relu = 1; y (BF16) and/or yf (FP32) receive it.
+ * use_tensor_cores = 1 runs the tcgen05 implicit GEMM with `wpk` (weights packed by
+ * fs_conv_pack_weights); 0 runs the CUDA-core reference with the FP32 weights `w32`
+ * ([co][tap][ci], 32 x 9 x 32). All pointers are device pointers; `err` (nullable) is
+ * set if a tensor-core wait gave up. */
+FS_API int fs_conv_pack_weights(const float* w32, void* wpk, void* stream);
+FS_API int fs_conv3x3(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip,
+                      void* y, float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores,
+                      int* err, void* stream);
+
+/* Remaining building blocks of the learned warm start (no counterpart in the reference),
+ * on device pointers, NHWC with 32 channels, images stacked along rows:
+ *   avgpool2 (BF16, rows_out x w_out output) and its backward (FP32, dx = dy/4 broadcast);
+ *   upsample2_bwd: dlow = 2x2 block sums of dup; relu_bwd: dz = (da + da2) * (a > 0),
+ *   FP32 and BF16 copies; weight_grad: dw += sum_p dz x im2col(x), db += sum_p dz (CUDA
+ *   cores, FP32 atomics); flip_weights: weights of the backward-data convolution;
+ *   mse: loss on channel 0 and its gradient (per-CTA partial sums of squared error);
+ *   adam: one Adam step on FP32 weights (frozen mask nullable);
+ *   restrict / prolong: fine pitched fields <-> the G x G network grid (see net.cu). */
+FS_API int fs_net_avgpool2(const void* x, void* y, int rows_out, int w_out, void* stream);
+FS_API int fs_net_avgpool2_bwd(const float* dy, float* dx, int rows_in, int w_in, void* stream);
+FS_API int fs_net_upsample2_bwd(const float* dup, float* dlow, int rows_low, int w_low, void* stream);
+FS_API int fs_net_relu_bwd(const float* da, const float* da2, const void* a, float* dz, void* dzb, long long n,
+                           int relu, void* stream);
+FS_API int fs_net_weight_grad(const float* dz, const void* x, float* dw, float* db, int H, int W, int img_h, int up,
+                              void* stream);
+FS_API int fs_net_flip_weights(const float* w, float* wt, void* stream);
+FS_API int fs_net_mse(const float* y, const float* target, float* dy, float* loss_part, long long n, void* stream);
+FS_API int fs_net_adam(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
+                       float eps, int step, const unsigned char* frozen, void* stream);
+FS_API int fs_net_restrict(const float* div, const float* p_prev, int rows, int cols, int pitch, int G, float kappa,
+                           float* scale, void* xin, float* pc, void* stream);
+FS_API int fs_net_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
+                          const float* scale, float kappa, void* stream);
 
 /* Pinned host memory helpers (page-locked; fastest fs_solve_host / upload / download). */
 FS_API int fs_host_alloc(void** ptr, unsigned long long bytes);
