@@ -111,6 +111,10 @@ SIGNATURES = {
     "fs_set_network": (C.c_int, [_P, _P, C.c_longlong]),
     "fs_capture_view": (C.c_int, [_P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "fs_memcpy_device": (C.c_int, [_P, _P, C.c_ulonglong, _P]),
+    "fs_render_density": (C.c_int, [_P, _I, _I, _I, _F, _F, _F, _P, _P]),
+    "fs_render_velocity_lines": (C.c_int, [_P, _P, _I, _I, _I, _F, _F, _P, _P]),
+    "fs_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
+    "fs_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
     "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
     "fs_host_free": (C.c_int, [_P]),
     "fs_version": (C.c_char_p, []),
@@ -260,6 +264,33 @@ class Solver:
         return {KIND_NAMES[k]: {"launches": t.launches[k], "ms": t.ms[k], "bytes": t.algorithmic_bytes[k]}
                 for k in range(FS_NUM_KINDS)}
 
+    def render_density(self, multipliers=(1.0, 1.0, 1.0)) -> np.ndarray:
+        """RGBA8 image (rows, cols, 4) of the resident density (grid_to_image_kernel)."""
+        v = self.device_view()
+        dev = _DeviceBuffer(self.rows * self.cols * 4)
+        _check(self._lib.fs_render_density(v.density, v.rows, v.cols, v.pitch, *map(float, multipliers), dev.ptr,
+                                           v.stream))
+        img = dev.to_host(v.stream).reshape(self.rows, self.cols, 4)
+        dev.free()
+        return img
+
+    def render_velocity_lines(self, hscale: float, vscale: float) -> np.ndarray:
+        """Line vertices (rows*cols*2 records of x, y, r, g, b, a, u, v) of the resident
+        velocity (velocity_to_lines_kernel)."""
+        v = self.device_view()
+        n = self.rows * self.cols * 2
+        dev = _DeviceBuffer(n * 20)
+        _check(self._lib.fs_render_velocity_lines(v.u, v.v, v.rows, v.cols, v.pitch, hscale, vscale, dev.ptr, v.stream))
+        raw = dev.to_host(v.stream)
+        dev.free()
+        return raw.view(VERTEX_DTYPE)
+
+    def save_checkpoint(self, path):
+        _check(self._lib.fs_checkpoint_save(self._h, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        _check(self._lib.fs_checkpoint_load(self._h, str(path).encode()))
+
     def set_network(self, params: np.ndarray):
         params = np.ascontiguousarray(params, np.float32)
         _check(self._lib.fs_set_network(self._h, params.ctypes.data, params.size))
@@ -364,6 +395,29 @@ class FluidSolverGPU(Solver):
 
     def __init__(self, rows: int, cols: int, **config):
         super().__init__(rows, cols, **config)
+
+
+VERTEX_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("r", "u1"), ("g", "u1"), ("b", "u1"), ("a", "u1"),
+                         ("u", "<f4"), ("v", "<f4")])
+
+
+class _DeviceBuffer:
+    """Raw device allocation through the CUDA runtime that the library links."""
+
+    def __init__(self, nbytes):
+        import torch
+
+        self._t = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        self.ptr = C.c_void_p(self._t.data_ptr())
+
+    def to_host(self, stream):
+        import torch
+
+        torch.cuda.synchronize()
+        return self._t.cpu().numpy()
+
+    def free(self):
+        self._t = None
 
 
 class PinnedArray:

@@ -140,46 +140,26 @@ __global__ void __launch_bounds__(256) advect_velocity_kernel(const float* __res
 }
 
 // ----------------------------------------------------------------- batched
-// One launch covers every grid of a batch: blocks of 32x8 cells are numbered grid
-// by grid (prefix[g] = first block of grid g) and each block finds its grid by binary
-// search. Persistent: the launch has a few waves' worth of CTAs that stride over all
-// blocks.
-
-constexpr int kSmemJobs = 2048;
-
-__device__ __forceinline__ int find_job(const int* __restrict__ sp, const int* __restrict__ prefix, int n, int b) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((n <= kSmemJobs ? sp[mid] : __ldg(prefix + mid)) <= b) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
+// One launch covers every grid of a batch: blocks of 32x8 cells are numbered grid by
+// grid (prefix[g] = first block of grid g, block_job[b] = grid of block b).
 
 template <int OP>
 __global__ void __launch_bounds__(256) advect_batch_kernel(const AdvectJob* __restrict__ jobs,
-                                                           const int* __restrict__ prefix, int njobs, int nblocks,
-                                                           int* nonfinite) {
-    // the block prefix is searched in shared memory when it fits
-    __shared__ int sp[kSmemJobs];
-    if (njobs <= kSmemJobs)
-        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < njobs; i += blockDim.x * blockDim.y) sp[i] = prefix[i];
-    __syncthreads();
+                                                           const int* __restrict__ prefix,
+                                                           const int* __restrict__ block_job, int* nonfinite) {
+    const int b = blockIdx.x;
+    const int g = __ldg(block_job + b);
+    const AdvectJob& J = jobs[g];
+    const int lb = b - __ldg(prefix + g);
+    const int bx = (J.A.cols + 31) / 32;
+    const int i = (lb / bx) * 8 + threadIdx.y, j = (lb % bx) * 32 + threadIdx.x;
     int bad = 0;
-    for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        const int g = find_job(sp, prefix, njobs, b);
-        const AdvectJob& J = jobs[g];
-        const int lb = b - __ldg(prefix + g);
-        const int bx = (J.A.cols + 31) / 32;
-        const int i = (lb / bx) * 8 + threadIdx.y, j = (lb % bx) * 32 + threadIdx.x;
-        if (OP == 0) {
-            if (i >= 1 && i < J.A.rows - 1 && j >= 1 && j < J.A.cols - 1) splat_cell(J.in0, J.in1, J.in2, J.out0, J.A, i, j);
-        } else if (OP == 1) {
-            if (i < J.A.rows && j < J.A.cols) bad |= finish_cell(J.in0, J.out0, J.smooth, J.A, i, j);
-        } else {
-            if (i < J.A.rows && j < J.A.cols) advect_cell(J.in0, J.in1, J.out0, J.out1, J.A, i, j);
-        }
+    if (OP == 0) {
+        if (i >= 1 && i < J.A.rows - 1 && j >= 1 && j < J.A.cols - 1) splat_cell(J.in0, J.in1, J.in2, J.out0, J.A, i, j);
+    } else if (OP == 1) {
+        if (i < J.A.rows && j < J.A.cols) bad = finish_cell(J.in0, J.out0, J.smooth, J.A, i, j);
+    } else {
+        if (i < J.A.rows && j < J.A.cols) advect_cell(J.in0, J.in1, J.out0, J.out1, J.A, i, j);
     }
     if (bad && nonfinite) atomicOr(nonfinite, 1);
 }
@@ -216,16 +196,15 @@ cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, f
 
 int advect_batch_blocks(int rows, int cols) { return ((cols + 31) / 32) * ((rows + 7) / 8); }
 
-cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, int njobs, int nblocks,
+cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                 int* nonfinite, cudaStream_t st) {
     if (nblocks <= 0) return cudaSuccess;
-    const int grid = std::min(nblocks, 152 * 8 * 4);
     if (op == 0)
-        advect_batch_kernel<0><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
+        advect_batch_kernel<0><<<nblocks, dim3(32, 8), 0, st>>>(jobs, prefix, block_job, nonfinite);
     else if (op == 1)
-        advect_batch_kernel<1><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
+        advect_batch_kernel<1><<<nblocks, dim3(32, 8), 0, st>>>(jobs, prefix, block_job, nonfinite);
     else
-        advect_batch_kernel<2><<<grid, dim3(32, 8), 0, st>>>(jobs, prefix, njobs, nblocks, nonfinite);
+        advect_batch_kernel<2><<<nblocks, dim3(32, 8), 0, st>>>(jobs, prefix, block_job, nonfinite);
     return cudaGetLastError();
 }
 

@@ -5,8 +5,8 @@
 // (fluid_solver_gpu.cu:222-404). A batch here advances every grid of the batch with
 // the same stage sequence as a single handle, but each sub-step is ONE launch over
 // all grids: the stencil passes walk a device-resident table of per-grid field
-// descriptors (tiles of all grids concatenated, persistent CTAs striding over them),
-// and the advection stages walk a table of per-grid jobs. The whole step is captured
+// descriptors (tiles of all grids concatenated, one CTA per tile, a tile -> field
+// map), and the advection stages walk a table of per-grid jobs (a block -> job map). The whole step is captured
 // once as a CUDA graph. Grids share dt, the rates and the sweep counts; each grid has
 // its own size, state and sources.
 //
@@ -57,14 +57,15 @@ struct fs_batch {
     std::vector<int> h_prefix;
     std::vector<AdvectJob> h_jobs;
     std::vector<int> h_jprefix;
+    std::vector<int> h_map;   // tile -> field for every pass, then block -> job for every op
     struct Pass {
-        size_t tab, prefix;  // offsets into the tables
+        size_t tab, prefix, map;  // offsets into the tables
         int nfields, total;
         bool diffuse;
     };
     std::vector<Pass> passes;  // diffusion passes, then project 1, then project 2
     int n_diffuse = 0, n_project = 0;
-    size_t job_off[3] = {}, jprefix_off[3] = {};
+    size_t job_off[3] = {}, jprefix_off[3] = {}, jmap_off[3] = {};
     int job_blocks[3] = {};
     void* d_plan = nullptr;
     size_t d_plan_bytes = 0;
@@ -72,6 +73,7 @@ struct fs_batch {
     int* d_prefix = nullptr;
     AdvectJob* d_jobs = nullptr;
     int* d_jprefix = nullptr;
+    int* d_map = nullptr;
     int launches_per_step = 0;
     fs_stats stats{};
 
@@ -88,6 +90,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     b->h_prefix.clear();
     b->h_jobs.clear();
     b->h_jprefix.clear();
+    b->h_map.clear();
     b->passes.clear();
     const int n = b->count;
     const int K = b->sweeps;
@@ -100,7 +103,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     const float rates[3] = {diff, visc, visc};
     const int modes[3] = {BND_CONT, BND_OPP_H, BND_OPP_V};
     for (size_t pass = 0; pass < dplan.size(); ++pass) {
-        fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), 0, 0, true};
+        fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, true};
         int tiles = 0;
         for (int g = 0; g < n; ++g)
             for (int q = 0; q < 3; ++q) {
@@ -124,6 +127,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 }
                 b->h_prefix.push_back(tiles);
                 tiles += f.tiles_x * f.tiles_y;
+                b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
                 b->h_tab.push_back(f);
                 P.nfields++;
             }
@@ -138,7 +142,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     for (int proj = 0; proj < 2; ++proj) {
         for (int pass = 0; pass < b->n_project; ++pass) {
             const bool last = pass == b->n_project - 1;
-            fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), 0, 0, false};
+            fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, false};
             int tiles = 0;
             for (int g = 0; g < n; ++g) {
                 StencilField f{};
@@ -171,6 +175,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 }
                 b->h_prefix.push_back(tiles);
                 tiles += f.tiles_x * f.tiles_y;
+                b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
                 b->h_tab.push_back(f);
                 P.nfields++;
             }
@@ -183,6 +188,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     for (int op = 0; op < 3; ++op) {
         b->job_off[op] = b->h_jobs.size();
         b->jprefix_off[op] = b->h_jprefix.size();
+        b->jmap_off[op] = b->h_map.size();
         int blocks = 0;
         for (int g = 0; g < n; ++g) {
             AdvectJob J{};
@@ -203,7 +209,9 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 J.out1 = b->fld(K_VEL_V, g);
             }
             b->h_jprefix.push_back(blocks);
-            blocks += advect_batch_blocks(b->rows[g], b->cols[g]);
+            const int nb = advect_batch_blocks(b->rows[g], b->cols[g]);
+            blocks += nb;
+            b->h_map.insert(b->h_map.end(), nb, g);
             b->h_jobs.push_back(J);
         }
         b->h_jprefix.push_back(blocks);
@@ -214,8 +222,9 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     const size_t pre_bytes = b->h_prefix.size() * sizeof(int);
     const size_t job_bytes = b->h_jobs.size() * sizeof(AdvectJob);
     const size_t jpre_bytes = b->h_jprefix.size() * sizeof(int);
+    const size_t map_bytes = b->h_map.size() * sizeof(int);
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t need = up(tab_bytes) + up(pre_bytes) + up(job_bytes) + up(jpre_bytes);
+    const size_t need = up(tab_bytes) + up(pre_bytes) + up(job_bytes) + up(jpre_bytes) + up(map_bytes);
     if (need > b->d_plan_bytes) {
         if (b->d_plan) cudaFree(b->d_plan);
         b->d_plan = nullptr;
@@ -228,16 +237,18 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     b->d_prefix = reinterpret_cast<int*>(base + up(tab_bytes));
     b->d_jobs = reinterpret_cast<AdvectJob*>(base + up(tab_bytes) + up(pre_bytes));
     b->d_jprefix = reinterpret_cast<int*>(base + up(tab_bytes) + up(pre_bytes) + up(job_bytes));
+    b->d_map = reinterpret_cast<int*>(base + up(tab_bytes) + up(pre_bytes) + up(job_bytes) + up(jpre_bytes));
     FS_CK(cudaMemcpyAsync(b->d_tab, b->h_tab.data(), tab_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaMemcpyAsync(b->d_prefix, b->h_prefix.data(), pre_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs.data(), job_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaMemcpyAsync(b->d_jprefix, b->h_jprefix.data(), jpre_bytes, cudaMemcpyHostToDevice, b->stream));
+    FS_CK(cudaMemcpyAsync(b->d_map, b->h_map.data(), map_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaStreamSynchronize(b->stream));  // host vectors may change before the next upload
     return FS_OK;
 }
 
 int enqueue_pass(fs_batch* b, const fs_batch::Pass& P, int& launches) {
-    FS_CK(launch_stencil_table(b->d_tab + P.tab, b->d_prefix + P.prefix, P.nfields, P.total, P.diffuse,
+    FS_CK(launch_stencil_table(b->d_tab + P.tab, b->d_prefix + P.prefix, b->d_map + P.map, P.total, P.diffuse,
                                b->tile_rows, b->stream));
     launches++;
     return FS_OK;
@@ -250,15 +261,15 @@ int enqueue_step(fs_batch* b, int& launches) {
         if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;
     FS_CK(cudaMemsetAsync(b->slab + (size_t)K_ACC * b->range_floats, 0, b->range_floats * sizeof(float), b->stream));
     int* nf = b->cfg.check_finite ? b->flags : nullptr;
-    FS_CK(launch_advect_batch(0, b->d_jobs + b->job_off[0], b->d_jprefix + b->jprefix_off[0], b->count,
-                              b->job_blocks[0], nullptr, b->stream));
-    FS_CK(launch_advect_batch(1, b->d_jobs + b->job_off[1], b->d_jprefix + b->jprefix_off[1], b->count,
-                              b->job_blocks[1], nf, b->stream));
+    FS_CK(launch_advect_batch(0, b->d_jobs + b->job_off[0], b->d_jprefix + b->jprefix_off[0],
+                              b->d_map + b->jmap_off[0], b->job_blocks[0], nullptr, b->stream));
+    FS_CK(launch_advect_batch(1, b->d_jobs + b->job_off[1], b->d_jprefix + b->jprefix_off[1],
+                              b->d_map + b->jmap_off[1], b->job_blocks[1], nf, b->stream));
     launches += 2;
     for (int k = 0; k < b->n_project; ++k)
         if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;
-    FS_CK(launch_advect_batch(2, b->d_jobs + b->job_off[2], b->d_jprefix + b->jprefix_off[2], b->count,
-                              b->job_blocks[2], nullptr, b->stream));
+    FS_CK(launch_advect_batch(2, b->d_jobs + b->job_off[2], b->d_jprefix + b->jprefix_off[2],
+                              b->d_map + b->jmap_off[2], b->job_blocks[2], nullptr, b->stream));
     launches++;
     for (int k = 0; k < b->n_project; ++k)
         if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;

@@ -145,12 +145,12 @@ cudaError_t launch_learned_select(const float* div, float* guess, const float* p
 
 int advect_batch_blocks(int rows, int cols);
 // op 0: splat, 1: density finish, 2: velocity backtrace; prefix[g] = first 32x8
-// block of job g (njobs + 1 entries, the last = nblocks).
-cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, int njobs, int nblocks,
+// block of job g, block_job[b] = job of block b.
+cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                 int* nonfinite, cudaStream_t st);
 // Stencil pass over a device table of fields (batched grids); prefix[f] = first tile
-// of field f, prefix[nfields] = total tiles.
-cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, int nfields, int total_tiles,
+// of field f, tile_field[t] = field of tile t.
+cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, const int* tile_field, int total_tiles,
                                  bool diffuse, int tile_rows, cudaStream_t st);
 cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
                                    cudaStream_t st);

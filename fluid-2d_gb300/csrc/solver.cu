@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -956,6 +957,65 @@ int fs_capture_view(fs_solver* s, int slot, float** div, float** p_start, float*
     if (p_start) *p_start = s->cap_start[slot];
     if (p_final) *p_final = s->cfg.warm_start != FS_WARM_ZERO ? s->pwarm[slot] : nullptr;
     if (!s->cfg.capture) return fail(FS_ERR_STATE, "fs_capture_view: the handle was created without capture");
+    return FS_OK;
+}
+
+namespace {
+struct CheckpointHeader {
+    char magic[8];
+    int32_t rows, cols, warm_valid, reserved;
+    int64_t steps;
+};
+static_assert(sizeof(CheckpointHeader) == 32, "checkpoint header layout");
+constexpr char kCkpMagic[8] = {'F', 'S', '2', 'D', 'C', 'K', 'P', '1'};
+}  // namespace
+
+int fs_checkpoint_save(fs_solver* s, const char* path) {
+    if (!s || !path) return fail(FS_ERR_ARG, "fs_checkpoint_save: null argument");
+    DeviceGuard g(s->device);
+    const size_t n = (size_t)s->rows * s->cols;
+    std::vector<float> buf(n * 8);
+    float* fields[8] = {s->st[F_D], s->st[F_U], s->st[F_V], s->src[F_D], s->src[F_U], s->src[F_V], s->pwarm[0],
+                        s->pwarm[1]};
+    for (int k = 0; k < 8; ++k) {
+        int rc = copy_out(s, buf.data() + k * n, fields[k]);
+        if (rc != FS_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    CheckpointHeader h{};
+    std::memcpy(h.magic, kCkpMagic, 8);
+    h.rows = s->rows;
+    h.cols = s->cols;
+    h.warm_valid = s->warm_valid ? 1 : 0;
+    h.steps = s->stats.steps;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(FS_ERR_ARG, "fs_checkpoint_save: cannot open the file");
+    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    std::fclose(f);
+    return ok ? FS_OK : fail(FS_ERR_ARG, "fs_checkpoint_save: write failed");
+}
+
+int fs_checkpoint_load(fs_solver* s, const char* path) {
+    if (!s || !path) return fail(FS_ERR_ARG, "fs_checkpoint_load: null argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(FS_ERR_ARG, "fs_checkpoint_load: cannot open the file");
+    CheckpointHeader h{};
+    const size_t n = (size_t)s->rows * s->cols;
+    std::vector<float> buf(n * 8);
+    bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCkpMagic, 8) == 0 && h.rows == s->rows &&
+              h.cols == s->cols && std::fread(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    std::fclose(f);
+    if (!ok) return fail(FS_ERR_ARG, "fs_checkpoint_load: not a checkpoint of this grid size");
+    DeviceGuard g(s->device);
+    float* fields[8] = {s->st[F_D], s->st[F_U], s->st[F_V], s->src[F_D], s->src[F_U], s->src[F_V], s->pwarm[0],
+                        s->pwarm[1]};
+    for (int k = 0; k < 8; ++k) {
+        int rc = copy_in(s, fields[k], buf.data() + k * n);
+        if (rc != FS_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->warm_valid = h.warm_valid != 0;
+    s->stats.steps = h.steps;
     return FS_OK;
 }
 

@@ -321,39 +321,24 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     process_tile<TY, SR, DIFF>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
 }
 
-// One pass over a device-resident table of fields (a batch of grids of uneven
-// size). Persistent: a few CTAs per SM stride over the concatenated tile list;
-// prefix[f] is the first tile of field f and each tile finds its field by binary
-// search. Tiles of all grids have the same shape, so the stride keeps SMs balanced.
+// One pass over a device-resident table of fields (a batch of grids of uneven size):
+// one CTA per tile of the concatenated tile list; tile_field[t] names the field of
+// tile t and prefix[f] its first tile. The field's descriptor is staged in shared
+// memory, where the tile body reads it many times.
 template <int TY, int SR, bool DIFF>
 __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
-    stencil_table_kernel(const StencilField* __restrict__ tab, const int* __restrict__ prefix, int nf, int total) {
-    // the tile prefix of up to kSmemPrefix fields is searched in shared memory
-    constexpr int kSmemPrefix = 2048;
-    __shared__ int sp[kSmemPrefix];
-    const bool in_smem = nf <= kSmemPrefix;
-    if (in_smem)
-        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nf; i += blockDim.x * blockDim.y) sp[i] = prefix[i];
+    stencil_table_kernel(const StencilField* __restrict__ tab, const int* __restrict__ prefix,
+                         const int* __restrict__ tile_field) {
+    __shared__ StencilField sF;
+    static_assert(sizeof(StencilField) % 4 == 0, "descriptor copied as words");
+    const int t = blockIdx.x;
+    const int f = __ldg(tile_field + t);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid < (int)(sizeof(StencilField) / 4))
+        reinterpret_cast<int*>(&sF)[tid] = __ldg(reinterpret_cast<const int*>(tab + f) + tid);
     __syncthreads();
-#pragma unroll 1
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        int lo = 0, hi = nf - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((in_smem ? sp[mid] : __ldg(prefix + mid)) <= t) lo = mid;
-            else hi = mid - 1;
-        }
-        // stage this grid's descriptor in shared memory (read many times per tile)
-        __shared__ StencilField sF;
-        static_assert(sizeof(StencilField) % 4 == 0, "descriptor copied as words");
-        __syncthreads();
-        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-        if (tid < (int)(sizeof(StencilField) / 4))
-            reinterpret_cast<int*>(&sF)[tid] = __ldg(reinterpret_cast<const int*>(tab + lo) + tid);
-        __syncthreads();
-        float rn = 0.f, rd = 0.f;
-        process_tile<TY, SR, DIFF>(sF, t - __ldg(prefix + lo), sF.x, sF.y, false, rn, rd);
-    }
+    float rn = 0.f, rd = 0.f;
+    process_tile<TY, SR, DIFF>(sF, t - __ldg(prefix + f), sF.x, sF.y, false, rn, rd);
 }
 
 // ---------------------------------------------------------------------------
@@ -511,23 +496,15 @@ cudaError_t prepare_variant() {
 }
 
 template <int TY, int SR>
-cudaError_t launch_table_variant(const StencilField* tab, const int* prefix, int nf, int total, bool diffuse,
-                                 cudaStream_t st) {
+cudaError_t launch_table_variant(const StencilField* tab, const int* prefix, const int* tile_field, int total,
+                                 bool diffuse, cudaStream_t st) {
     if (total <= 0) return cudaSuccess;
-    int dev = 0, sms = 0, per = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stencil_table_kernel<TY, SR, false>, kRegionW * TY,
-                                                          smem_bytes<TY, SR>());
-    if (e != cudaSuccess) return e;
-    const int grid = std::max(1, std::min(total, per * sms));
     if (diffuse)
-        stencil_table_kernel<TY, SR, true><<<grid, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix, nf,
-                                                                                                    total);
+        stencil_table_kernel<TY, SR, true><<<total, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix,
+                                                                                                     tile_field);
     else
-        stencil_table_kernel<TY, SR, false><<<grid, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix, nf,
-                                                                                                     total);
+        stencil_table_kernel<TY, SR, false><<<total, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix,
+                                                                                                      tile_field);
     return cudaGetLastError();
 }
 
@@ -601,10 +578,10 @@ cudaError_t launch_pressure_solve(const PressureSolve& P, int tile_rows, int blo
     return launch_solve_variant<4, 16>(P, blocks, st);
 }
 
-cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, int nfields, int total_tiles,
+cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, const int* tile_field, int total_tiles,
                                  bool diffuse, int tile_rows, cudaStream_t st) {
-    if (tile_rows == 128) return launch_table_variant<8, 16>(table, prefix, nfields, total_tiles, diffuse, st);
-    return launch_table_variant<4, 16>(table, prefix, nfields, total_tiles, diffuse, st);
+    if (tile_rows == 128) return launch_table_variant<8, 16>(table, prefix, tile_field, total_tiles, diffuse, st);
+    return launch_table_variant<4, 16>(table, prefix, tile_field, total_tiles, diffuse, st);
 }
 
 }  // namespace fs

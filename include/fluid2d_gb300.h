@@ -150,6 +150,26 @@ FS_API int fs_capture_view(fs_solver* s, int slot, float** div, float** p_start,
 /* Device-to-device copy on a stream (helper for callers holding raw device pointers). */
 FS_API int fs_memcpy_device(void* dst, const void* src, unsigned long long bytes, void* stream);
 
+/* Headless render kernels on device fields (rows x pitch floats), for the
+ * reference's display path without its SFML window:
+ *   fs_render_density: RGBA8 image, rows*cols*4 bytes, as grid_to_image_kernel
+ *     (src/density_grid_renderer.cu:10-29);
+ *   fs_render_velocity_lines: 2 vertices per cell in sf::Vertex layout (x, y floats,
+ *     RGBA bytes, u, v texture floats = 20 bytes), as velocity_to_lines_kernel
+ *     (src/velocity_grid_renderer.cu:8-44). Outputs are device buffers. */
+FS_API int fs_render_density(const float* density, int rows, int cols, int pitch, float mr, float mg, float mb,
+                             void* rgba, void* stream);
+FS_API int fs_render_velocity_lines(const float* u, const float* v, int rows, int cols, int pitch, float hscale,
+                                    float vscale, void* vertices, void* stream);
+
+/* Checkpoint / resume (no counterpart in the reference). File layout, little endian:
+ *   char magic[8] = "FS2DCKP1"; int32 rows, cols, warm_valid, reserved; int64 steps;
+ *   then rows*cols float32 each of density, u, v, sources (3), warm-start pressures (2).
+ * fs_checkpoint_load needs a handle of the same rows/cols; it restores the state, the
+ * sources, the warm-start pressures and the step counter. */
+FS_API int fs_checkpoint_save(fs_solver* s, const char* path);
+FS_API int fs_checkpoint_load(fs_solver* s, const char* path);
+
 /* Single stages of the step on the resident state, for kernel-level checks. The
  * stage runs with the handle's sweep counts and leaves its result in the state. */
 #define FS_STAGE_DIFFUSE_DENSITY 1  /* add_sources + diffuse (fluid_solver_gpu.cu:237-238) */

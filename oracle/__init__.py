@@ -189,3 +189,41 @@ def rel_linf(x, y, skip_corners=True):
     if den == 0.0:
         return float(num)
     return float(num / den)
+
+
+# ---------------------------------------------------------------- render kernels
+
+def render_density(d, multipliers):
+    """grid_to_image_kernel (src/density_grid_renderer.cu:10-29): per channel
+    uint8(max(0, min(255, m * d))) truncating toward zero, alpha 255; NaN -> 255."""
+    d = np.asarray(d, np.float32)
+    out = np.empty(d.shape + (4,), np.uint8)
+    for c, m in enumerate(multipliers):
+        x = np.float32(m) * d
+        x = np.where(np.isnan(x), np.float32(255.0), np.minimum(np.float32(255.0), x))
+        out[..., c] = np.maximum(np.float32(0.0), x).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+def render_velocity_lines(u, v, hscale, vscale):
+    """velocity_to_lines_kernel (src/velocity_grid_renderer.cu:8-44): (rows*cols*2)
+    vertices (x, y, r, g, b, a, u, v) in float32/uint8, row-major, start then end."""
+    u = np.asarray(u, np.float32)
+    v = np.asarray(v, np.float32)
+    rows, cols = u.shape
+    ii, jj = np.meshgrid(np.arange(rows, dtype=np.float32), np.arange(cols, dtype=np.float32), indexing="ij")
+    sx = jj * np.float32(hscale)
+    sy = ii * np.float32(vscale)
+    norm = np.sqrt(np.float32(rows * cols))
+    mark = (np.arange(rows)[:, None] % 8 == 0) & (np.arange(cols)[None, :] % 8 == 0)
+    ex = np.where(mark, sx + (np.float32(250000.0) * u) / norm, sx).astype(np.float32)
+    ey = np.where(mark, sy + (np.float32(250000.0) * v) / norm, sy).astype(np.float32)
+    dt = np.dtype([("x", "<f4"), ("y", "<f4"), ("r", "u1"), ("g", "u1"), ("b", "u1"), ("a", "u1"),
+                   ("u", "<f4"), ("v", "<f4")])
+    out = np.zeros(rows * cols * 2, dt)
+    out["x"][0::2], out["y"][0::2] = sx.ravel(), sy.ravel()
+    out["x"][1::2], out["y"][1::2] = ex.ravel(), ey.ravel()
+    for c in "rgba":
+        out[c] = 255
+    return out
