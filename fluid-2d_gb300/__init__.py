@@ -25,6 +25,7 @@ from . import build_lib
 FS_OK, FS_ERR_ARG, FS_ERR_CUDA, FS_ERR_NONFINITE, FS_ERR_NOT_CONVERGED, FS_ERR_TIMEOUT, FS_ERR_NOMEM, \
     FS_ERR_STATE = range(8)
 FS_WARM_ZERO, FS_WARM_PREVIOUS, FS_WARM_LEARNED = 0, 1, 2
+FS_METHOD_JACOBI, FS_METHOD_GAUSS_SEIDEL = 0, 1
 STAGE_DIFFUSE_DENSITY, STAGE_ADVECT_DENSITY, STAGE_DIFFUSE_VELOCITY, STAGE_PROJECT, STAGE_ADVECT_VELOCITY = 1, 2, 3, 4, 5
 
 LIB_PATH = build_lib.LIB
@@ -41,7 +42,7 @@ class fs_config(C.Structure):
                 ("pressure_iterations", C.c_int), ("smooth", C.c_int), ("sweeps_per_pass", C.c_int),
                 ("tile_rows", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("warm_start", C.c_int),
                 ("pressure_tolerance", C.c_float), ("pressure_max_iterations", C.c_int),
-                ("check_finite", C.c_int), ("capture", C.c_int)]
+                ("check_finite", C.c_int), ("capture", C.c_int), ("method", C.c_int)]
 
 
 class fs_stats(C.Structure):
@@ -118,6 +119,7 @@ SIGNATURES = {
     "fs_host_alloc": (C.c_int, [C.POINTER(_P), C.c_ulonglong]),
     "fs_host_free": (C.c_int, [_P]),
     "fs_version": (C.c_char_p, []),
+    "fs_gauss_seidel_max_size": (C.c_int, [C.POINTER(C.c_int)]),
 }
 
 _lib = None
@@ -395,6 +397,25 @@ class FluidSolverGPU(Solver):
 
     def __init__(self, rows: int, cols: int, **config):
         super().__init__(rows, cols, **config)
+
+
+class FluidSolverGaussSeidel(Solver):
+    """Drop-in for the reference's fluid_solver_cpu (src/fluid_solver_cpu.hpp:8-50) that
+    runs on the GPU and returns the host solver's results bit for bit: square grids only
+    (the host solver's grid reads cols as rows), 20 diffusion and 20 pressure sweeps."""
+
+    def __init__(self, n: int, **config):
+        config.setdefault("diffuse_iterations", 20)
+        config.setdefault("pressure_iterations", 20)
+        config.setdefault("smooth", 0)
+        super().__init__(n, n, method=FS_METHOD_GAUSS_SEIDEL, **config)
+
+
+def gauss_seidel_max_size() -> int:
+    """Largest grid side the Gauss-Seidel method accepts on the current device."""
+    n = C.c_int(0)
+    _check(load().fs_gauss_seidel_max_size(C.byref(n)))
+    return n.value
 
 
 VERTEX_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("r", "u1"), ("g", "u1"), ("b", "u1"), ("a", "u1"),

@@ -155,4 +155,16 @@ cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, c
 cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
                                    cudaStream_t st);
 
+// Gauss-Seidel compatibility step (gs.cu): the host solver's method, bit for bit, on a
+// square n x n grid of pitched fields; three scratch fields of the same shape.
+struct GsFields {
+    float *d, *u, *v;
+    const float *ds, *us, *vs;
+    float* scratch[3];
+};
+int gs_max_size();                 // largest n on the current device
+cudaError_t gs_prepare();          // shared-memory opt-in on the current device, outside capture
+cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float diff, float visc, float dt,
+                    cudaStream_t st);
+
 }  // namespace fs

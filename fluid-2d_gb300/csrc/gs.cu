@@ -1,0 +1,348 @@
+// Exact reproduction of the reference's host solver (fluid_solver_cpu, src/
+// fluid_solver_cpu.cpp:6-215) on the GPU, for square grids whose field fits in one
+// SM's shared memory (n <= gs_max_size(), 234 on a 227 KB part).
+//
+// The host solver differs from the CUDA one in method, not just rounding: its
+// diffusion and pressure sweeps update in place in row-major order (lexicographic
+// Gauss-Seidel), every boundary fill also averages the four corners, the diffusion
+// divisor is float, there is no smoothing, and the forward splat adds in raster order.
+// Here each in-place solve runs in one CTA with the field in shared memory as an
+// anti-diagonal wavefront: cell (i, j) of sweep s is updated at time (i-1)+(j-1)+2s, so
+// every sweep sees its up/left neighbours already updated and its down/right
+// neighbours not yet, exactly as the sequential loop does, and all sweeps are in
+// flight at once. An edge cell is read only by its inner neighbour, so the thread that
+// updates that neighbour also rewrites the edge (the fill the host solver does after
+// every sweep); corners are never read by a sweep and are averaged once at the end.
+// The splat keeps raster order: the whole CTA computes the targets and weights of a
+// chunk of source cells, one thread then applies them in order.
+//
+// A step is four launches on the solver's pitched fields (element (i, j) at i*P + j):
+//   1. 3 CTAs: add sources + diffuse d | copy u, add sources, diffuse u | same for v
+//   2. 2 CTAs: splat d by the step's initial velocity (the copies) | project u, v
+//   3. 1 CTA : copy u, v; advect both by the copies (gather)
+//   4. 1 CTA : project u, v
+// Every operation uses explicitly rounded single-precision intrinsics so that no
+// contraction changes a result; the outputs are bit-identical to the host solver's.
+
+#include <cuda_runtime.h>
+
+#include "../../include/fluid2d_gb300.h"
+#include "fs_internal.cuh"
+
+namespace fs {
+namespace {
+
+constexpr int kGsThreads = 1024;
+constexpr int kGsStage = 512;  // source cells per splat chunk
+
+struct GsStageEntry {
+    int i0, j0;
+    float w[4];  // contributions to (i0,j0), (i0+1,j0), (i0,j0+1), (i0+1,j0+1)
+};
+
+// set_boundary_* of the host solver (fluid_solver_cpu.cpp:33-83) on an n x n field of
+// row stride `ld`: edges from their inner neighbours with the mode's signs, then the
+// corners averaged from their two edge neighbours. Ends with a block barrier.
+__device__ void cpu_fill(float* g, int n, int ld, int mode) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float s_lr = mode == BND_OPP_H ? -1.f : 1.f, s_tb = mode == BND_OPP_V ? -1.f : 1.f;
+    for (int k = 1 + tid; k < n - 1; k += nt) {
+        g[k * ld] = s_lr * g[k * ld + 1];
+        g[k * ld + n - 1] = s_lr * g[k * ld + n - 2];
+        g[k] = s_tb * g[ld + k];
+        g[(n - 1) * ld + k] = s_tb * g[(n - 2) * ld + k];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const int b = (n - 1) * ld, c = n - 1;
+        g[0] = __fmul_rn(0.5f, __fadd_rn(g[1], g[ld]));
+        g[c] = __fmul_rn(0.5f, __fadd_rn(g[c - 1], g[ld + c]));
+        g[b] = __fmul_rn(0.5f, __fadd_rn(g[b + 1], g[b - ld]));
+        g[b + c] = __fmul_rn(0.5f, __fadd_rn(g[b + c - 1], g[b - ld + c]));
+    }
+    __syncthreads();
+}
+
+// Pipelined lexicographic Gauss-Seidel on x (shared, n x n dense, in place):
+//   DIFF: x = (c + a*(U + D + L + R)) / den          (fluid_solver_cpu.cpp:105-110)
+//   else: x = (c + R + L + D + U) / 4                (fluid_solver_cpu.cpp:197-202)
+// with c read from `cst` (global, row stride P): x0 for diffusion, div for pressure.
+template <bool DIFF>
+__device__ void gs_wavefront(float* x, const float* cst, int n, int P, int iters, int mode, float a, float den) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float s_lr = mode == BND_OPP_H ? -1.f : 1.f, s_tb = mode == BND_OPP_V ? -1.f : 1.f;
+    const int m = n - 2, dmax = 2 * m - 2;
+    const int last_t = dmax + 2 * (iters - 1);
+    for (int t = 0; t <= last_t; ++t) {
+        // sweeps with a diagonal d = t - 2s in [0, dmax]
+        const int s_lo = t > dmax ? (t - dmax + 1) / 2 : 0;
+        const int s_hi = min(iters - 1, t / 2);
+        const int work = (s_hi - s_lo + 1) * m;
+        for (int e = tid; e < work; e += nt) {
+            const int s = s_lo + e / m, q = e % m, d = t - 2 * s;
+            if (q < d - (m - 1) || q > d) continue;
+            const int i = 1 + q, j = 1 + d - q;
+            const int o = i * n + j;
+            float val;
+            if (DIFF) {
+                float sum = __fadd_rn(x[o - n], x[o + n]);
+                sum = __fadd_rn(sum, x[o - 1]);
+                sum = __fadd_rn(sum, x[o + 1]);
+                val = __fdiv_rn(__fadd_rn(cst[i * P + j], __fmul_rn(a, sum)), den);
+            } else {
+                float sum = __fadd_rn(cst[i * P + j], x[o + 1]);
+                sum = __fadd_rn(sum, x[o - 1]);
+                sum = __fadd_rn(sum, x[o + n]);
+                sum = __fadd_rn(sum, x[o - n]);
+                val = __fdiv_rn(sum, 4.0f);
+            }
+            x[o] = val;
+            // the host solver's fill after this sweep, for the edges next to (i, j)
+            if (j == 1) x[o - 1] = s_lr * val;
+            if (j == n - 2) x[o + 1] = s_lr * val;
+            if (i == 1) x[o - n] = s_tb * val;
+            if (i == n - 2) x[o + n] = s_tb * val;
+        }
+        __syncthreads();
+    }
+}
+
+struct GsArgs {
+    float* f[3];         // d, u, v (state)
+    const float* src[3]; // ds, us, vs
+    float* su;           // scratch: copy of u
+    float* sv;           // scratch: copy of v
+    float* dv;           // scratch: divergence
+    int n, P, kd, kp;
+    float a[3], den[3];  // diffusion constants per field
+    float dt, dt0, h;
+};
+
+__device__ void copy_field(float* dst, const float* src, int n, int P) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) dst[(e / n) * P + e % n] = src[(e / n) * P + e % n];
+}
+
+// add_source then diffuse (fluid_solver_cpu.cpp:85-114) of field k.
+__device__ void gs_diffuse(const GsArgs& A, int k, float* x) {
+    const int n = A.n, P = A.P;
+    const int mode = k == 0 ? BND_CONT : (k == 1 ? BND_OPP_H : BND_OPP_V);
+    float* g = A.f[k];
+    const float* s = A.src[k];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n, o = i * P + j;
+        float val = g[o];
+        if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+            val = __fadd_rn(val, __fmul_rn(A.dt, s[o]));
+            g[o] = val;  // the diffusion's x0
+        }
+        x[e] = val;
+    }
+    __syncthreads();
+    if (A.kd > 0) {
+        gs_wavefront<true>(x, g, n, P, A.kd, mode, A.a[k], A.den[k]);
+        cpu_fill(x, n, n, mode);
+    }
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) g[(e / n) * P + e % n] = x[e];
+}
+
+// advect(trace=true) (fluid_solver_cpu.cpp:127-152) of d by (su, sv), accumulating in
+// shared memory, then the host solver's continuous fill.
+__device__ void gs_splat(const GsArgs& A, float* acc, GsStageEntry* stage) {
+    const int n = A.n, P = A.P, m = n - 2;
+    const float* d0 = A.f[0];
+    const float hi = (float)n - 1.5f;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) acc[e] = 0.f;
+    for (int base = 0; base < m * m; base += kGsStage) {
+        const int cnt = min(kGsStage, m * m - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+            const int c = base + k, i = 1 + c / m, j = 1 + c % m, o = i * P + j;
+            const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
+            const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
+            GsStageEntry en;
+            if (x < 0.5f || x > hi || y < 0.5f || y > hi) {
+                en.i0 = -1;
+                en.j0 = 0;
+                en.w[0] = en.w[1] = en.w[2] = en.w[3] = 0.f;
+            } else {
+                const int j0 = (int)x, i0 = (int)y;
+                const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+                const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+                const float w = d0[o];
+                en.i0 = i0;
+                en.j0 = j0;
+                en.w[0] = __fmul_rn(__fmul_rn(s1, s3), w);
+                en.w[1] = __fmul_rn(__fmul_rn(s1, s2), w);
+                en.w[2] = __fmul_rn(__fmul_rn(s0, s3), w);
+                en.w[3] = __fmul_rn(__fmul_rn(s0, s2), w);
+            }
+            stage[k] = en;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < cnt; ++k) {
+                const GsStageEntry en = stage[k];
+                if (en.i0 < 0) continue;
+                const int t = en.i0 * n + en.j0;
+                acc[t] = __fadd_rn(acc[t], en.w[0]);
+                acc[t + n] = __fadd_rn(acc[t + n], en.w[1]);
+                acc[t + 1] = __fadd_rn(acc[t + 1], en.w[2]);
+                acc[t + n + 1] = __fadd_rn(acc[t + n + 1], en.w[3]);
+            }
+        }
+    }
+    __syncthreads();
+    cpu_fill(acc, n, n, BND_CONT);
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A.f[0][(e / n) * P + e % n] = acc[e];
+}
+
+// project (fluid_solver_cpu.cpp:179-215) of (u, v), pressure from zero in shared memory.
+__device__ void gs_project(const GsArgs& A, float* p) {
+    const int n = A.n, P = A.P, m = n - 2;
+    float* u = A.f[1];
+    float* v = A.f[2];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) p[e] = 0.f;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int o = (1 + e / m) * P + 1 + e % m;
+        float s = __fsub_rn(u[o + 1], u[o - 1]);
+        s = __fadd_rn(s, v[o + P]);
+        s = __fsub_rn(s, v[o - P]);
+        A.dv[o] = __fmul_rn(__fmul_rn(-0.5f, A.h), s);
+    }
+    __syncthreads();
+    if (A.kp > 0) {
+        gs_wavefront<false>(p, A.dv, n, P, A.kp, BND_CONT, 0.f, 0.f);
+        cpu_fill(p, n, n, BND_CONT);
+    }
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int i = 1 + e / m, j = 1 + e % m, o = i * P + j, q = i * n + j;
+        u[o] = __fsub_rn(u[o], __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(p[q + 1], p[q - 1])), A.h));
+        v[o] = __fsub_rn(v[o], __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(p[q + n], p[q - n])), A.h));
+    }
+    __syncthreads();
+    cpu_fill(u, n, P, BND_OPP_H);
+    cpu_fill(v, n, P, BND_OPP_V);
+}
+
+// advect(trace=false) (fluid_solver_cpu.cpp:154-173) of u and v by the copies (su, sv).
+__device__ void gs_gather(const GsArgs& A) {
+    const int n = A.n, P = A.P, m = n - 2;
+    copy_field(A.su, A.f[1], n, P);
+    copy_field(A.sv, A.f[2], n, P);
+    __syncthreads();
+    const float hi = (float)n - 1.5f;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int i = 1 + e / m, j = 1 + e % m, o = i * P + j;
+        float x = __fsub_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
+        float y = __fsub_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
+        x = (x < hi) ? x : hi;
+        x = (1.5f < x) ? x : 1.5f;
+        y = (y < hi) ? y : hi;
+        y = (1.5f < y) ? y : 1.5f;
+        const int j0 = (int)x, i0 = (int)y;
+        const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+        const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+        const int a = i0 * P + j0;
+        for (int k = 0; k < 2; ++k) {
+            const float* g0 = k == 0 ? A.su : A.sv;
+            const float top = __fadd_rn(__fmul_rn(s1, g0[a]), __fmul_rn(s0, g0[a + 1]));
+            const float bot = __fadd_rn(__fmul_rn(s1, g0[a + P]), __fmul_rn(s0, g0[a + P + 1]));
+            A.f[1 + k][o] = __fadd_rn(__fmul_rn(s3, top), __fmul_rn(s2, bot));
+        }
+    }
+    __syncthreads();
+    cpu_fill(A.f[1], n, P, BND_OPP_H);
+    cpu_fill(A.f[2], n, P, BND_OPP_V);
+}
+
+__global__ void __launch_bounds__(kGsThreads) gs_diffuse_kernel(const __grid_constant__ GsArgs A) {
+    extern __shared__ float4 gs_smem[];
+    float* x = reinterpret_cast<float*>(gs_smem);
+    const int k = blockIdx.x;
+    if (k > 0) {  // keep the step's initial velocity for the density splat
+        copy_field(k == 1 ? A.su : A.sv, A.f[k], A.n, A.P);
+        __syncthreads();
+    }
+    gs_diffuse(A, k, x);
+}
+
+__global__ void __launch_bounds__(kGsThreads) gs_splat_project_kernel(const __grid_constant__ GsArgs A) {
+    extern __shared__ float4 gs_smem[];
+    float* f = reinterpret_cast<float*>(gs_smem);
+    if (blockIdx.x == 0)
+        gs_splat(A, f, reinterpret_cast<GsStageEntry*>(f + A.n * A.n));
+    else
+        gs_project(A, f);
+}
+
+__global__ void __launch_bounds__(kGsThreads) gs_gather_kernel(const __grid_constant__ GsArgs A) { gs_gather(A); }
+
+__global__ void __launch_bounds__(kGsThreads) gs_project_kernel(const __grid_constant__ GsArgs A) {
+    extern __shared__ float4 gs_smem[];
+    gs_project(A, reinterpret_cast<float*>(gs_smem));
+}
+
+size_t gs_smem_bytes(int n) {
+    return ((size_t)n * n * sizeof(float) + 15) / 16 * 16 + kGsStage * sizeof(GsStageEntry);
+}
+
+}  // namespace
+
+int gs_max_size() {
+    int dev = 0, smem = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+    int n = 3;
+    while (gs_smem_bytes(n + 1) <= (size_t)smem) ++n;
+    return n;
+}
+
+cudaError_t gs_prepare() {
+    // the largest size, so that handles of different sizes share one setting
+    const int n = gs_max_size();
+    if (n < 3) return cudaErrorNoDevice;
+    const int bytes = (int)gs_smem_bytes(n);
+    cudaError_t e = cudaFuncSetAttribute(gs_diffuse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(gs_splat_project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(gs_project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e;
+}
+
+cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float diff, float visc, float dt,
+                    cudaStream_t st) {
+    GsArgs A;
+    A.f[0] = F.d;
+    A.f[1] = F.u;
+    A.f[2] = F.v;
+    A.src[0] = F.ds;
+    A.src[1] = F.us;
+    A.src[2] = F.vs;
+    A.su = F.scratch[0];
+    A.sv = F.scratch[1];
+    A.dv = F.scratch[2];
+    A.n = n;
+    A.P = pitch;
+    A.kd = kd;
+    A.kp = kp;
+    // constants as the host solver computes them, in float (fluid_solver_cpu.cpp:97-98,
+    // 119, 181): a = dt * (rows*cols) * rate, den = 1 + 4a, dt0 = sqrt(rows*cols) * dt
+    const float cells = (float)((size_t)n * (size_t)n);
+    const float rates[3] = {diff, visc, visc};
+    for (int k = 0; k < 3; ++k) {
+        A.a[k] = dt * cells * rates[k];
+        A.den[k] = 1.f + 4.f * A.a[k];  // 4a is exact, so a fused form rounds the same
+    }
+    A.dt = dt;
+    A.dt0 = sqrtf(cells) * dt;
+    A.h = 1.0f / sqrtf(cells);
+    const size_t smem = gs_smem_bytes(n);
+    gs_diffuse_kernel<<<3, kGsThreads, smem, st>>>(A);
+    gs_splat_project_kernel<<<2, kGsThreads, smem, st>>>(A);
+    gs_gather_kernel<<<1, kGsThreads, 0, st>>>(A);
+    gs_project_kernel<<<1, kGsThreads, smem, st>>>(A);
+    return cudaGetLastError();
+}
+
+}  // namespace fs

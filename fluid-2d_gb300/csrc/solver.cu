@@ -504,6 +504,20 @@ int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const fl
 
 int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
     int rc;
+    if (s->cfg.method == FS_METHOD_GAUSS_SEIDEL) {
+        GsFields F;
+        F.d = s->st[F_D];
+        F.u = s->st[F_U];
+        F.v = s->st[F_V];
+        F.ds = s->src[F_D];
+        F.us = s->src[F_U];
+        F.vs = s->src[F_V];
+        for (int k = 0; k < 3; ++k) F.scratch[k] = s->x0[k];
+        CK(gs_step(F, s->rows, s->pitch, s->cfg.diffuse_iterations, s->cfg.pressure_iterations, diff, visc, dt,
+                   s->stream));
+        cnt.launches += 4;
+        return FS_OK;
+    }
     // density and velocity diffusion are independent; one launch per pass serves all three
     const int fields[3] = {F_D, F_U, F_V};
     const float rates[3] = {diff, visc, visc};
@@ -674,6 +688,17 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         return fail(FS_ERR_ARG, "fs_create: pressure_tolerance must be >= 0");
     if (cfg->pressure_tolerance > 0.f && cfg->pressure_max_iterations < 1)
         return fail(FS_ERR_ARG, "fs_create: pressure_max_iterations must be >= 1 with a residual target");
+    if (cfg->method != FS_METHOD_JACOBI && cfg->method != FS_METHOD_GAUSS_SEIDEL)
+        return fail(FS_ERR_ARG, "fs_create: unknown method");
+    if (cfg->method == FS_METHOD_GAUSS_SEIDEL) {
+        // the host solver's grid is square (its cols() returns rows, src/grid.hpp:20-22),
+        // its pressure starts from zero and its sweep counts are fixed
+        if (cfg->rows != cfg->cols)
+            return fail(FS_ERR_ARG, "fs_create: the Gauss-Seidel method needs a square grid");
+        if (cfg->warm_start != FS_WARM_ZERO || cfg->pressure_tolerance > 0.f || cfg->capture)
+            return fail(FS_ERR_ARG,
+                        "fs_create: the Gauss-Seidel method takes no warm start, residual target or capture");
+    }
 
     fs_solver* s = new fs_solver();
     s->cfg = *cfg;
@@ -694,8 +719,13 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     const int maxk = stencil_max_halo(s->tile_rows) - 1;
     s->sweeps = cfg->sweeps_per_pass > 0 ? std::min(cfg->sweeps_per_pass, maxk) : std::min(8, maxk);
 
+    if (cfg->method == FS_METHOD_GAUSS_SEIDEL && cfg->rows > gs_max_size()) {
+        delete s;
+        return fail(FS_ERR_ARG, "fs_create: grid too large for the Gauss-Seidel method (fs_gauss_seidel_max_size)");
+    }
     cudaError_t e = stencil_prepare();
     if (e == cudaSuccess) e = pressure_solve_max_blocks(s->tile_rows, &s->solve_blocks);
+    if (e == cudaSuccess && cfg->method == FS_METHOD_GAUSS_SEIDEL) e = gs_prepare();
     if (e != cudaSuccess) {
         delete s;
         return cuda_fail(e, "fs_create: stencil kernel set-up");
@@ -785,6 +815,12 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     return FS_OK;
 }
 
+int fs_gauss_seidel_max_size(int* n) {
+    if (!n) return fail(FS_ERR_ARG, "fs_gauss_seidel_max_size: null argument");
+    *n = gs_max_size();
+    return *n > 0 ? FS_OK : fail(FS_ERR_CUDA, "fs_gauss_seidel_max_size: no CUDA device");
+}
+
 int fs_destroy(fs_solver* s) {
     if (!s) return FS_OK;
     DeviceGuard g(s->device);
@@ -859,6 +895,7 @@ int fs_solve_host(fs_solver* s, float* density, const float* density_source, flo
 
 int fs_stage(fs_solver* s, int stage, float rate, float dt) {
     if (!s) return fail(FS_ERR_ARG, "fs_stage: null handle");
+    if (s->cfg.method != FS_METHOD_JACOBI) return fail(FS_ERR_STATE, "fs_stage: Jacobi method only");
     DeviceGuard g(s->device);
     Counter cnt;
     int rc = FS_OK;
@@ -904,6 +941,7 @@ int fs_stage(fs_solver* s, int stage, float rate, float dt) {
 
 int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, fs_kernel_times* out) {
     if (!s || !out) return fail(FS_ERR_ARG, "fs_profile_step: null argument");
+    if (s->cfg.method != FS_METHOD_JACOBI) return fail(FS_ERR_STATE, "fs_profile_step: Jacobi method only");
     DeviceGuard g(s->device);
     std::memset(out, 0, sizeof(*out));
     s->prof = out;

@@ -52,6 +52,16 @@ extern "C" {
 #define FS_WARM_PREVIOUS 1
 #define FS_WARM_LEARNED 2 /* network correction of the previous pressure (fs_set_network) */
 
+/* Solution method of the step. FS_METHOD_JACOBI is the reference's CUDA solver
+ * (fluid_solver_gpu, src/fluid_solver_gpu.cu:209-404). FS_METHOD_GAUSS_SEIDEL reproduces
+ * the reference's host solver (fluid_solver_cpu, src/fluid_solver_cpu.cpp:6-215) bit for
+ * bit: in-place lexicographic sweeps, corner-averaging fills, no smoothing. It needs a
+ * square grid of at most fs_gauss_seidel_max_size() cells a side, pressure from zero and a
+ * fixed iteration count; the host solver uses 20 diffusion and 20 pressure sweeps
+ * (src/fluid_solver_cpu.cpp:14,24). */
+#define FS_METHOD_JACOBI 0
+#define FS_METHOD_GAUSS_SEIDEL 1
+
 typedef struct fs_solver fs_solver;
 
 typedef struct fs_config {
@@ -70,6 +80,7 @@ typedef struct fs_config {
     int check_finite;          /* 1: flag NaN/Inf in the step's outputs (FS_ERR_NONFINITE) */
     int capture;               /* 1: keep each projection's divergence and starting pressure
                                   for fs_capture_view (training-data generation) */
+    int method;                /* FS_METHOD_JACOBI (default) or FS_METHOD_GAUSS_SEIDEL */
 } fs_config;
 
 typedef struct fs_stats {
@@ -106,6 +117,11 @@ FS_API int fs_config_init(fs_config* cfg, int rows, int cols);
 /* Replaces fluid_solver_gpu::fluid_solver_gpu(rows, cols) (fluid_solver_gpu.cu:209-218):
  * allocates the device state for one grid. */
 FS_API int fs_create(const fs_config* cfg, fs_solver** out);
+
+/* Largest grid side (rows = cols, boundary included) that FS_METHOD_GAUSS_SEIDEL accepts
+ * on the calling thread's current device: one field must fit in one SM's shared memory.
+ * Writes 0 when no device is usable. */
+FS_API int fs_gauss_seidel_max_size(int* n);
 
 /* Replaces fluid_solver_gpu::~fluid_solver_gpu (fluid_solver_gpu.cu:220). NULL is a no-op. */
 FS_API int fs_destroy(fs_solver* s);

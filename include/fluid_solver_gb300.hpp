@@ -61,3 +61,52 @@ private:
 
     fs_solver* m_handle = nullptr;
 };
+
+// Drop-in for the reference's fluid_solver_cpu (src/fluid_solver_cpu.hpp:11-50): the host
+// solver's method (in-place Gauss-Seidel, corner-averaging fills, 20 + 20 sweeps,
+// src/fluid_solver_cpu.cpp:6-31), run on the GPU with bit-identical results. Like the
+// reference class it is default-constructed and takes its size from the grids passed to
+// solve(); the device state is created on the first call and again when the size
+// changes. Square grids up to fs_gauss_seidel_max_size() a side.
+// simulation.cpp:18-20 becomes
+//     m_solver = std::make_unique<fluid_solver_gb300_gauss_seidel>();
+class fluid_solver_gb300_gauss_seidel : public fluid_solver {
+public:
+    fluid_solver_gb300_gauss_seidel() = default;
+    fluid_solver_gb300_gauss_seidel(const fluid_solver_gb300_gauss_seidel&) = delete;
+    fluid_solver_gb300_gauss_seidel& operator=(const fluid_solver_gb300_gauss_seidel&) = delete;
+    ~fluid_solver_gb300_gauss_seidel() override { fs_destroy(m_handle); }
+
+    void solve(grid<float>& density_grid, grid<float> const& density_source_grid, float const diffusion_rate,
+               grid<float>& horizontal_velocity_grid, grid<float>& vertical_velocity_grid,
+               grid<float> const& horizontal_velocity_source_grid,
+               grid<float> const& vertical_velocity_source_grid, float const viscosity, float const dt) override {
+        const int n = (int)density_grid.rows();
+        if (!m_handle || n != m_n) {
+            fs_destroy(m_handle);
+            m_handle = nullptr;
+            fs_config cfg;
+            check(fs_config_init(&cfg, n, n));
+            cfg.method = FS_METHOD_GAUSS_SEIDEL;
+            cfg.diffuse_iterations = 20;
+            cfg.pressure_iterations = 20;
+            cfg.smooth = 0;
+            check(fs_create(&cfg, &m_handle));
+            m_n = n;
+        }
+        check(fs_solve_host(m_handle, density_grid.data(), density_source_grid.data(), diffusion_rate,
+                            horizontal_velocity_grid.data(), vertical_velocity_grid.data(),
+                            horizontal_velocity_source_grid.data(), vertical_velocity_source_grid.data(),
+                            viscosity, dt));
+    }
+
+    fs_solver* handle() const { return m_handle; }
+
+private:
+    static void check(int rc) {
+        if (rc != FS_OK) throw std::runtime_error(std::string("fluid2d_gb300: ") + fs_last_error());
+    }
+
+    fs_solver* m_handle = nullptr;
+    int m_n = 0;
+};

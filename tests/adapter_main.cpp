@@ -12,9 +12,13 @@
 int main(int argc, char** argv) {
     const std::size_t n = 34;
     const int steps = argc > 1 ? std::atoi(argv[1]) : 3;
+    const bool gauss_seidel = argc > 2 && argv[2][0] == 'g';
     std::unique_ptr<fluid_solver> solver;
     try {
-        solver = std::make_unique<fluid_solver_gb300>(n, n);
+        if (gauss_seidel)
+            solver = std::make_unique<fluid_solver_gb300_gauss_seidel>();
+        else
+            solver = std::make_unique<fluid_solver_gb300>(n, n);
     } catch (const std::runtime_error& e) {
         std::printf("create failed: %s\n", e.what());
         return 3;

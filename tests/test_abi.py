@@ -98,6 +98,7 @@ def test_adapter_builds_against_reference_headers(fluid, tmp_path):
 @pytest.mark.gpu
 def test_adapter_runs_like_the_reference_app(fluid, tmp_path):
     exe = _build_adapter(tmp_path, [ROOT / "tests" / "ref_iface"])
-    r = subprocess.run([str(exe), "4"], capture_output=True, text=True)
-    assert r.returncode == 0, r.stdout + r.stderr
-    assert "mass" in r.stdout
+    for mode in ("jacobi", "gauss-seidel"):
+        r = subprocess.run([str(exe), "4", mode], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "mass" in r.stdout
