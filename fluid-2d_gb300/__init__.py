@@ -42,7 +42,8 @@ class fs_config(C.Structure):
                 ("pressure_iterations", C.c_int), ("smooth", C.c_int), ("sweeps_per_pass", C.c_int),
                 ("tile_rows", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("warm_start", C.c_int),
                 ("pressure_tolerance", C.c_float), ("pressure_max_iterations", C.c_int),
-                ("check_finite", C.c_int), ("capture", C.c_int), ("method", C.c_int)]
+                ("check_finite", C.c_int), ("capture", C.c_int), ("method", C.c_int),
+                ("learned_cycles", C.c_int), ("learned_cycle_iterations", C.c_int)]
 
 
 class fs_stats(C.Structure):
@@ -107,7 +108,7 @@ SIGNATURES = {
     "fs_net_flip_weights": (C.c_int, [_P, _P, _P]),
     "fs_net_mse": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P]),
     "fs_net_adam": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _F, _F, _F, _F, _I, _P, _P]),
-    "fs_net_restrict": (C.c_int, [_P, _P, _I, _I, _I, _I, _F, _P, _P, _P, _P]),
+    "fs_net_restrict": (C.c_int, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
     "fs_net_prolong": (C.c_int, [_P, _P, _P, _I, _I, _I, _I, _P, _F, _P]),
     "fs_set_network": (C.c_int, [_P, _P, C.c_longlong]),
     "fs_capture_view": (C.c_int, [_P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),

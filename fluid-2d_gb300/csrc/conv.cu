@@ -52,6 +52,7 @@ struct ConvArgs {
     int up;                    // 1: the input is nearest-upsampled by 2 on the fly
     int relu;
     int* err;                  // set to 1 if an mbarrier wait gave up
+    const int* skip_if;        // nullable: when *skip_if != 0 the launch does nothing
 };
 
 // Source pixel of tap (dy, dx) for output pixel (y, x), or -1 outside its image.
@@ -112,6 +113,7 @@ __global__ void __launch_bounds__(128) conv3x3_tc_kernel(const ConvArgs P) {
     uint8_t* Bs = sm + kAbytes;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kAbytes + kBbytes);
     uint32_t* s_taddr = reinterpret_cast<uint32_t*>(sm + kAbytes + kBbytes + 16);
+    if (P.skip_if && __ldcg(P.skip_if)) return;  // uniform across the CTA, before any TMEM use
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long npix = (long)P.H * P.W;
     const long p0 = (long)blockIdx.x * kTileM;
@@ -178,6 +180,7 @@ __global__ void __launch_bounds__(128) conv3x3_tc_kernel(const ConvArgs P) {
 
 // Reference: one thread per (pixel, output channel), FP32 accumulation of BF16 values.
 __global__ void __launch_bounds__(256) conv3x3_ref_kernel(const ConvArgs P, const float* __restrict__ w32) {
+    if (P.skip_if && __ldcg(P.skip_if)) return;
     const long npix = (long)P.H * P.W;
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npix) return;
@@ -229,6 +232,13 @@ extern "C" int fs_conv_pack_weights(const float* w32, void* wpk, void* stream) {
 extern "C" int fs_conv3x3(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip,
                           void* y, float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores,
                           int* err, void* stream) {
+    return fs::conv3x3_launch(x, wpk, w32, bias, skip, y, yf, H, W, img_h, up, relu, use_tensor_cores, err, nullptr,
+                              stream);
+}
+
+int fs::conv3x3_launch(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip, void* y,
+                       float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores, int* err,
+                       const int* skip_if, void* stream) {
     if (!x || H < 1 || W < 1 || (!y && !yf)) return record_error(FS_ERR_ARG, "fs_conv3x3: bad argument");
     if (img_h <= 0) img_h = H;
     if (H % img_h != 0) return record_error(FS_ERR_ARG, "fs_conv3x3: H must be a multiple of img_h");
@@ -246,6 +256,7 @@ extern "C" int fs_conv3x3(const void* x, const void* wpk, const float* w32, cons
     P.up = up;
     P.relu = relu;
     P.err = err;
+    P.skip_if = skip_if;
     cudaStream_t st = (cudaStream_t)stream;
     const long npix = (long)H * W;
     if (use_tensor_cores) {

@@ -82,6 +82,11 @@ struct SolveCtrl {
 // launch: `first` (divergence fused) then `mid` passes until the relative residual
 // drops to tol or max_passes ran, then `fin` (zero sweeps: gradient subtract and
 // reflecting fills). Passes ping-pong between p[0] and p[1].
+//
+// Segment mode (learned corrections): the divergence already exists, `first` is a
+// PASS_PRESSURE field whose x is p_cur and `fin` is unused. The launch does nothing if
+// ctrl->converged is already set; otherwise it runs passes from p_cur until the target
+// or max_passes and copies the final pressure back to p_cur. ctrl->passes accumulates.
 struct PressureSolve {
     StencilField first, mid, fin;
     float* p[2];
@@ -90,6 +95,8 @@ struct PressureSolve {
     SolveCtrl* ctrl;
     float tol;
     int max_passes;
+    int segment;                    // 1: segment mode
+    float* p_cur;                   // segment: start and final pressure
 };
 
 // Semi-Lagrangian advection parameters.
@@ -137,11 +144,31 @@ cudaError_t launch_density_finish(const float* acc, float* d, int smooth, const 
                                   cudaStream_t st);
 // Tensor-core conv set-up (shared-memory opt-in) on the current device (conv.cu).
 cudaError_t conv_prepare();
+// fs_conv3x3 with a skip flag: when skip_if (nullable) points at a non-zero value the
+// launch does nothing (a converged pressure solve skips its remaining corrections).
+int conv3x3_launch(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip, void* y,
+                   float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores, int* err,
+                   const int* skip_if, void* stream);
 
-// Learned warm start: residuals of the network's guess and of the previous pressure,
-// then keep the better one in `guess` (net.cu).
-cudaError_t launch_learned_select(const float* div, float* guess, const float* prev, int rows, int cols, int pitch,
-                                  double* res2, unsigned long long* counters, cudaStream_t st);
+// Learned corrections (net.cu). Coarse residual: block sums of the residual of p (null =
+// zero) into bs[G*G], their squared norm into *norm2 and, when xin is given, the network
+// input and its scale. Coarse smoothing: nu weighted-Jacobi sweeps of the coarse
+// equation 4e_I - sum(e_J) = bs_I (Neumann) from channel 0 of y_in (null = zero) into
+// channel 0 of y_out. Energy gain: adds to *out how much closer p_try is to the solution
+// than p_cur in the A-norm (2 c.r - c.Ac, c = p_try - p_cur). Accept: unless *converged,
+// p_cur becomes pa or pb when its gain (gain[0], gain[1]) is the larger positive one;
+// counters[0] counts pa chosen, counters[1] otherwise. Every launcher takes a nullable
+// skip flag with the meaning of conv3x3_launch's.
+cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, int cols, int pitch, int G, float* bs,
+                                   double* norm2, float* scale, void* xin, const int* skip_if, cudaStream_t st);
+cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* bs, const float* scale, float kappa,
+                                 int G, int nu, const int* skip_if, cudaStream_t st);
+cudaError_t launch_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
+                           const float* scale, float kappa, const int* skip_if, cudaStream_t st);
+cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float* p_try, int rows, int cols,
+                               int pitch, double* out, const int* skip_if, cudaStream_t st);
+cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, long n_floats, const double* gain,
+                               const int* converged, unsigned long long* counters, cudaStream_t st);
 
 int advect_batch_blocks(int rows, int cols);
 // op 0: splat, 1: density finish, 2: velocity backtrace; prefix[g] = first 32x8

@@ -1,11 +1,11 @@
 // Elementwise, pooling, gradient and optimizer kernels of the learned pressure warm
 // start, and the fine <-> coarse transfers that connect it to the pressure solve.
 //
-// The network runs on a fixed coarse grid (G x G cells, G = FS_NET_GRID): each coarse
-// cell covers an R x R block of the fine interior (R = N / G). The coarse problem is
-// L_c p_c = sum of the fine divergence over the block, whose solution approximates the
-// block mean of the fine pressure, so a network trained at one fine size applies to
-// others. Activations are NHWC with 32 channels; gradients are FP32.
+// The network runs on a coarse grid (G x G cells, G = FS_NET_GRID): each coarse cell
+// covers an R x R block of the fine interior (R = N / G). Its input is the block sum of
+// the Poisson residual of the current pressure; its output is the block mean of the
+// correction that solves the residual equation, L_c e_c = block sums of r, so a network
+// trained at one fine size applies to others and to any starting pressure. Activations are NHWC with 32 channels; gradients are FP32.
 //
 // No counterpart in the reference (it has no learned component).
 
@@ -179,23 +179,31 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
 }
 
 // ------------------------------------------------------- fine <-> coarse
-// Network input from the fine interior (pitched fields, rows x pitch, interior
-// 1..N): coarse cell (I, J) of a G x G grid covers an R x R block. Channel 0 = block
-// SUM of div divided by `scale`, channel 1 = block MEAN of p_prev divided by
-// (scale * kappa), channels 2..31 = 0. Also writes the FP32 coarse p_prev mean.
+// Block sums of the Poisson residual r = div + sum(nbrs p) - 4p of a starting pressure
+// p (pitched, edges filled; null = zero, r = div) over the fine interior 1..N: coarse
+// cell (I, J) of the G x G grid covers an R x R block. One CTA per coarse cell writes
+// the FP32 sum to bs[cell] and, when pc is given, the block MEAN of p to pc[cell].
+// The coarse correction that makes p exact solves L_c e_c = bs, so the residual alone
+// carries what the network needs from the divergence and the starting pressure.
 __global__ void restrict_kernel(const float* __restrict__ div, const float* __restrict__ p, int pitch, int R, int G,
-                                const float* __restrict__ scale_ptr, float kappa, __nv_bfloat16* __restrict__ xin,
-                                float* __restrict__ pc) {
-    const int cell = blockIdx.x;  // one CTA per coarse cell
+                                float* __restrict__ bs, float* __restrict__ pc, const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    const int cell = blockIdx.x;
     const int I = cell / G, J = cell % G;
-    float sd = 0.f, sp = 0.f;
+    float sr = 0.f, sp = 0.f;
     for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
         const int i = 1 + I * R + e / R, j = 1 + J * R + e % R;
-        sd += div[(size_t)i * pitch + j];
-        sp += p ? p[(size_t)i * pitch + j] : 0.f;
+        const size_t o = (size_t)i * pitch + j;
+        float r = div[o];
+        if (p) {
+            const float c = p[o];
+            r += (p[o - 1] + p[o + 1]) + (p[o - pitch] + p[o + pitch]) - 4.f * c;
+            sp += c;
+        }
+        sr += r;
     }
     __shared__ float a[256], b[256];
-    a[threadIdx.x] = sd;
+    a[threadIdx.x] = sr;
     b[threadIdx.x] = sp;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
@@ -205,35 +213,81 @@ __global__ void restrict_kernel(const float* __restrict__ div, const float* __re
         }
         __syncthreads();
     }
-    if (threadIdx.x < kC) {
-        const float scale = *scale_ptr;
-        const float mean_p = b[0] / (float)(R * R);
-        float v = 0.f;
-        if (threadIdx.x == 0) v = a[0] / scale;
-        if (threadIdx.x == 1) v = mean_p / (scale * kappa);
-        xin[(size_t)cell * kC + threadIdx.x] = __float2bfloat16_rn(v);
-        if (threadIdx.x == 0 && pc) pc[cell] = mean_p;
+    if (threadIdx.x == 0) {
+        bs[cell] = a[0];
+        if (pc) pc[cell] = b[0] / (float)(R * R);
     }
 }
 
-// RMS of the block sums of div over the coarse grid (one CTA), with a floor; the
-// network's input scale.
-__global__ void coarse_scale_kernel(const float* __restrict__ div, int pitch, int R, int G, float* __restrict__ out) {
-    __shared__ double red[256];
+// Network input from the block sums (one CTA): scale = RMS of bs with a floor,
+// channel 0 = bs / scale, channels 1..31 = 0 (xin nullable); *norm2 = sum of bs^2
+// (nullable).
+__global__ void coarse_input_kernel(const float* __restrict__ bs, int G, float* __restrict__ scale_out,
+                                    __nv_bfloat16* __restrict__ xin, double* __restrict__ norm2,
+                                    const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    __shared__ double red[1024];
+    __shared__ float s_scale;
     double acc = 0.0;
-    for (int cell = threadIdx.x; cell < G * G; cell += blockDim.x) {
-        const int I = cell / G, J = cell % G;
-        float s = 0.f;
-        for (int e = 0; e < R * R; ++e) s += div[(size_t)(1 + I * R + e / R) * pitch + 1 + J * R + e % R];
-        acc += (double)s * s;
-    }
+    for (int c = threadIdx.x; c < G * G; c += blockDim.x) acc += (double)bs[c] * bs[c];
     red[threadIdx.x] = acc;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = (float)fmax(sqrt(red[0] / (double)(G * G)), 1e-30);
+    if (threadIdx.x == 0) {
+        s_scale = (float)fmax(sqrt(red[0] / (double)(G * G)), 1e-30);
+        if (scale_out) *scale_out = s_scale;
+        if (norm2) *norm2 = red[0];
+    }
+    __syncthreads();
+    if (!xin) return;
+    const float inv = 1.f / s_scale;
+    for (int e = threadIdx.x; e < G * G * kC; e += blockDim.x)
+        xin[e] = __float2bfloat16_rn((e % kC) == 0 ? bs[e / kC] * inv : 0.f);
+}
+
+// Coarse post-smoothing of a coarse correction (one CTA, G*G <= 4096): e = y_in[.,0] *
+// scale * kappa (y_in null: e = 0), then nu sweeps of e_I <- (1-w) e_I + w (bs_I + sum
+// of the four neighbours) / 4, a missing neighbour reflecting e_I (Neumann), w = 0.8;
+// the mean is removed (the coarse problem's null space) and y_out[.,0] = e / (scale *
+// kappa) written (y_out may equal y_in). Applied to the network's output it removes the
+// cell-to-cell error that the fine sweeps would otherwise damp slowly; applied to zero it
+// is the classical coarse correction the network has to beat.
+constexpr int kCoarseMax = 64;
+__global__ void coarse_smooth_kernel(const float* y_in, float* y_out, const float* __restrict__ bs,
+                                     const float* __restrict__ scale_ptr, float kappa, int G, int nu,
+                                     const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    __shared__ float e[2][kCoarseMax * kCoarseMax];
+    __shared__ double red[1024];
+    const float unit = (*scale_ptr) * kappa;
+    for (int c = threadIdx.x; c < G * G; c += blockDim.x) e[0][c] = y_in ? y_in[(size_t)c * kC] * unit : 0.f;
+    __syncthreads();
+    const float w = 0.8f;
+    int cur = 0;
+    for (int it = 0; it < nu; ++it) {
+        for (int c = threadIdx.x; c < G * G; c += blockDim.x) {
+            const int I = c / G, J = c % G;
+            const float x = e[cur][c];
+            const float up = I > 0 ? e[cur][c - G] : x, dn = I < G - 1 ? e[cur][c + G] : x;
+            const float lf = J > 0 ? e[cur][c - 1] : x, rt = J < G - 1 ? e[cur][c + 1] : x;
+            e[cur ^ 1][c] = (1.f - w) * x + w * 0.25f * (bs[c] + up + dn + lf + rt);
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    double acc = 0.0;
+    for (int c = threadIdx.x; c < G * G; c += blockDim.x) acc += e[cur][c];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    const float mean = (float)(red[0] / (double)(G * G));
+    for (int c = threadIdx.x; c < G * G; c += blockDim.x) y_out[(size_t)c * kC] = (e[cur][c] - mean) / unit;
 }
 
 // Fine warm start: p_out = p_prev + bilinear interpolation of the coarse correction
@@ -241,7 +295,8 @@ __global__ void coarse_scale_kernel(const float* __restrict__ div, int pitch, in
 // edges take their inner neighbour (Neumann fill), corners keep p_prev.
 __global__ void prolong_kernel(const float* __restrict__ y, const float* __restrict__ p_prev, float* __restrict__ p_out,
                                int rows, int cols, int pitch, int R, int G, const float* __restrict__ scale_ptr,
-                               float kappa) {
+                               float kappa, const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
     const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long)rows * cols) return;
     const int i = (int)(e / cols), j = (int)(e % cols);
@@ -265,62 +320,94 @@ __global__ void prolong_kernel(const float* __restrict__ y, const float* __restr
     p_out[(size_t)i * pitch + j] = base + corr * (*scale_ptr) * kappa;
 }
 
-// Squared Poisson residuals ||div + sum(nbrs) - 4p||^2 of two pressures over the
-// interior (pb may be null = zero), accumulated into out[0], out[1] (zeroed before).
-__global__ void residual_pair_kernel(const float* __restrict__ div, const float* __restrict__ pa,
-                                     const float* __restrict__ pb, int rows, int cols, int pitch,
-                                     double* __restrict__ out) {
-    __shared__ double ra[256], rb[256];
-    double a = 0.0, b = 0.0;
+
+// Energy-norm gain of a candidate pressure p_try over p_cur: with c = p_try - p_cur and
+// the residual r = div + sum(nbrs p_cur) - 4 p_cur, the error e = A^-1 r (A the Neumann
+// 5-point operator, symmetric) changes by ||e - c||_A^2 = ||e||_A^2 - (2 c.r - c.Ac), so
+// gain = 2 c.r - c.Ac (interior sums, FP64 partials) is exactly how much closer p_try is
+// to the solution than p_cur in the norm the Jacobi iteration contracts. Accumulated
+// into *out (zeroed before).
+__global__ void energy_gain_kernel(const float* __restrict__ div, const float* __restrict__ p_cur,
+                                   const float* __restrict__ p_try, int rows, int cols, int pitch,
+                                   double* __restrict__ out, const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    __shared__ double red[256];
+    double g = 0.0;
     const long n = (long)(rows - 2) * (cols - 2);
     for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         const int i = 1 + (int)(e / (cols - 2)), j = 1 + (int)(e % (cols - 2));
         const size_t o = (size_t)i * pitch + j;
-        const float d = div[o];
-        const float s1 = d + pa[o - 1] + pa[o + 1] + pa[o - pitch] + pa[o + pitch] - 4.f * pa[o];
-        a += (double)s1 * s1;
-        float s2 = d;
-        if (pb) s2 += pb[o - 1] + pb[o + 1] + pb[o - pitch] + pb[o + pitch] - 4.f * pb[o];
-        b += (double)s2 * s2;
+        const float pc = p_cur[o];
+        const float r = div[o] + (p_cur[o - 1] + p_cur[o + 1]) + (p_cur[o - pitch] + p_cur[o + pitch]) - 4.f * pc;
+        const float c = p_try[o] - pc;
+        const float cl = p_try[o - 1] - p_cur[o - 1], cr = p_try[o + 1] - p_cur[o + 1];
+        const float cu = p_try[o - pitch] - p_cur[o - pitch], cd = p_try[o + pitch] - p_cur[o + pitch];
+        const float ac = 4.f * c - ((cl + cr) + (cu + cd));
+        g += 2.0 * (double)c * r - (double)c * ac;
     }
-    ra[threadIdx.x] = a;
-    rb[threadIdx.x] = b;
+    red[threadIdx.x] = g;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            ra[threadIdx.x] += ra[threadIdx.x + s];
-            rb[threadIdx.x] += rb[threadIdx.x + s];
-        }
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        atomicAdd(out, ra[0]);
-        atomicAdd(out + 1, rb[0]);
-    }
+    if (threadIdx.x == 0) atomicAdd(out, red[0]);
 }
 
-// Keep the network's guess when its residual is not larger than the previous
-// pressure's; otherwise overwrite the guess with the previous pressure (or zero).
-// counters[0] counts guesses used, counters[1] fallbacks.
-__global__ void select_guess_kernel(float* __restrict__ guess, const float* __restrict__ prev, long n_floats,
-                                    const double* __restrict__ res, unsigned long long* __restrict__ counters) {
-    const bool fallback = res[0] > res[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + (fallback ? 1 : 0), 1ull);
-    if (!fallback) return;
-    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n_floats; e += (long)gridDim.x * blockDim.x)
-        guess[e] = prev ? prev[e] : 0.f;
+// Keep the candidate with the largest positive energy gain (see launch_accept_best).
+__global__ void accept_best_kernel(float* __restrict__ p_cur, const float* __restrict__ pa,
+                                   const float* __restrict__ pb, long n4, const double* __restrict__ gain,
+                                   const int* __restrict__ converged, unsigned long long* __restrict__ counters) {
+    if (converged && __ldcg(converged)) return;
+    int pick = 0;
+    double best = 0.0;
+    if (gain[0] > best) {
+        pick = 1;
+        best = gain[0];
+    }
+    if (gain[1] > best) pick = 2;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + (pick == 1 ? 0 : 1), 1ull);
+    if (pick == 0) return;
+    const float4* src = reinterpret_cast<const float4*>(pick == 1 ? pa : pb);
+    float4* dst = reinterpret_cast<float4*>(p_cur);
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n4; e += (long)gridDim.x * blockDim.x)
+        dst[e] = src[e];
 }
 
 }  // namespace
 
-cudaError_t launch_learned_select(const float* div, float* guess, const float* prev, int rows, int cols, int pitch,
-                                  double* res2, unsigned long long* counters, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(res2, 0, 2 * sizeof(double), st);
-    if (e != cudaSuccess) return e;
-    residual_pair_kernel<<<152 * 4, 256, 0, st>>>(div, guess, prev, rows, cols, pitch, res2);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    select_guess_kernel<<<152 * 4, 256, 0, st>>>(guess, prev, (long)rows * pitch, res2, counters);
+cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, int cols, int pitch, int G, float* bs,
+                                   double* norm2, float* scale, void* xin, const int* skip_if, cudaStream_t st) {
+    const int R = (rows - 2) / G;
+    restrict_kernel<<<G * G, 256, 0, st>>>(div, p, pitch, R, G, bs, nullptr, skip_if);
+    coarse_input_kernel<<<1, 1024, 0, st>>>(bs, G, scale, (__nv_bfloat16*)xin, norm2, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* bs, const float* scale, float kappa,
+                                 int G, int nu, const int* skip_if, cudaStream_t st) {
+    if (G > kCoarseMax) return cudaErrorInvalidValue;
+    coarse_smooth_kernel<<<1, 1024, 0, st>>>(y_in, y_out, bs, scale, kappa, G, nu, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
+                           const float* scale, float kappa, const int* skip_if, cudaStream_t st) {
+    const long n = (long)rows * cols;
+    prolong_kernel<<<blocks_for(n, 256), 256, 0, st>>>(y, p_prev, p_out, rows, cols, pitch, (rows - 2) / G, G, scale,
+                                                       kappa, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float* p_try, int rows, int cols,
+                               int pitch, double* out, const int* skip_if, cudaStream_t st) {
+    energy_gain_kernel<<<152 * 4, 256, 0, st>>>(div, p_cur, p_try, rows, cols, pitch, out, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, long n_floats, const double* gain,
+                               const int* converged, unsigned long long* counters, cudaStream_t st) {
+    accept_best_kernel<<<152 * 4, 256, 0, st>>>(p_cur, pa, pb, n_floats / 4, gain, converged, counters);
     return cudaGetLastError();
 }
 
@@ -390,14 +477,14 @@ int fs_net_adam(float* w, const float* g, float* m, float* v, long long n, float
     return launched("fs_net_adam");
 }
 
-int fs_net_restrict(const float* div, const float* p_prev, int rows, int cols, int pitch, int G, float kappa,
+int fs_net_restrict(const float* div, const float* p_prev, int rows, int cols, int pitch, int G, float* work,
                     float* scale, void* xin, float* pc, void* stream) {
     const int N = rows - 2;
-    if (rows != cols || N % G != 0) return record_error(FS_ERR_ARG, "fs_net_restrict: N must be a multiple of G");
+    if (rows != cols || N % G != 0 || !work) return record_error(FS_ERR_ARG, "fs_net_restrict: N must be a multiple of G");
     const int R = N / G;
     cudaStream_t st = (cudaStream_t)stream;
-    coarse_scale_kernel<<<1, 256, 0, st>>>(div, pitch, R, G, scale);
-    restrict_kernel<<<G * G, 256, 0, st>>>(div, p_prev, pitch, R, G, scale, kappa, (__nv_bfloat16*)xin, pc);
+    restrict_kernel<<<G * G, 256, 0, st>>>(div, p_prev, pitch, R, G, work, pc, nullptr);
+    coarse_input_kernel<<<1, 1024, 0, st>>>(work, G, scale, (__nv_bfloat16*)xin, nullptr, nullptr);
     return launched("fs_net_restrict");
 }
 
@@ -407,7 +494,7 @@ int fs_net_prolong(const float* y, const float* p_prev, float* p_out, int rows, 
     if (rows != cols || N % G != 0) return record_error(FS_ERR_ARG, "fs_net_prolong: N must be a multiple of G");
     const long n = (long)rows * cols;
     prolong_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(y, p_prev, p_out, rows, cols, pitch, N / G,
-                                                                         G, scale, kappa);
+                                                                         G, scale, kappa, nullptr);
     return launched("fs_net_prolong");
 }
 

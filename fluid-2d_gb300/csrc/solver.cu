@@ -114,10 +114,13 @@ struct fs_solver {
         float* scale = nullptr;
         int* err = nullptr;
         unsigned long long* counters = nullptr;  // [guess used, fallback]
-        double* res = nullptr;            // two squared residuals
+        double* res = nullptr;            // [coarse residual norm^2, energy gain: network, coarse only]
+        float* bs = nullptr;              // coarse residual block sums of the current pressure, G*G
+        float* yc = nullptr;              // coarse-only correction, G*G*32 (channel 0 used)
         void* mem = nullptr;
     } net;
     float* pguess = nullptr;  // fine starting pressure built from the network
+    SolveCtrl* host_ctrl = nullptr;  // pinned mirror of a control block (learned cycles)
     bool net_ready = false;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -289,11 +292,8 @@ __nv_bfloat16* net_act(fs_solver* s, int k) {
     return s->net.act + off;
 }
 
-// Starting pressure of one projection from the network: divergence-only pass,
-// restriction to the coarse grid, the 8-layer network on the tensor cores,
-// interpolation of its correction onto the previous pressure, and the residual
-// comparison that keeps the previous pressure when the guess is worse.
-int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, int slot, Counter& cnt) {
+// Divergence of (u_in, v_in) into s->div: a pressure pass of zero sweeps.
+int enqueue_div_pass(fs_solver* s, const float* u_in, const float* v_in, Counter& cnt) {
     const float h = grid_h(s->rows, s->cols);
     StencilLaunch L{};
     L.nfields = 1;
@@ -309,16 +309,29 @@ int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, in
     f.cst_out = s->div;
     CK(launch_stencil(L, s->tile_rows, s->stream));
     cnt.launches++;
-    const float* prev = s->warm_valid ? s->pwarm[slot] : nullptr;
-    int rc = fs_net_restrict(s->div, prev, s->rows, s->cols, s->pitch, kNetG, kNetKappa, s->net.scale, net_act(s, 0),
-                             nullptr, s->stream);
-    if (rc != FS_OK) return rc;
+    return FS_OK;
+}
+
+constexpr int kCoarseSweeps = 20;
+
+// One learned correction of p_cur (the current pressure, edges filled): the block sums
+// of its residual on the coarse grid, the 8-layer network on the tensor cores, coarse
+// post-smoothing, bilinear interpolation into a candidate p_cur + correction; beside it
+// the classical candidate (the coarse smoothing from zero, no network). The judge keeps
+// the candidate that brings p_cur closest to the solution in the A-norm (the norm the
+// Jacobi iteration contracts), or p_cur when neither gets closer, and counts whether the
+// network's candidate won. Does nothing to p_cur once *converged (nullable) is set.
+int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged, Counter& cnt) {
+    CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, kNetG, s->net.bs, s->net.res, s->net.scale,
+                              net_act(s, 0), converged, s->stream));
     cnt.launches += 2;
+    int rc;
     auto conv = [&](int li, int in, int out, int lvl, int up, int skip, int relu, float* yf) {
         const int g = kNetG >> lvl;
-        return fs_conv3x3(net_act(s, in), s->net.wpk + (size_t)li * 9216, nullptr, s->net.params + (size_t)li * kNetLayer + 9216,
-                          skip >= 0 ? net_act(s, skip) : nullptr, out >= 0 ? net_act(s, out) : nullptr, yf, g, g, g, up,
-                          relu, 1, s->net.err, s->stream);
+        return conv3x3_launch(net_act(s, in), s->net.wpk + (size_t)li * 9216, nullptr,
+                              s->net.params + (size_t)li * kNetLayer + 9216, skip >= 0 ? net_act(s, skip) : nullptr,
+                              out >= 0 ? net_act(s, out) : nullptr, yf, g, g, g, up, relu, 1, s->net.err, converged,
+                              s->stream);
     };
     // e1 (G) -> pool -> e2, e3 (G/2) -> pool -> b1, b2 (G/4) -> d1 (+e3) -> d2 (+e1) -> out
     if ((rc = conv(0, 0, 1, 0, 0, -1, 1, nullptr)) != FS_OK) return rc;
@@ -332,13 +345,32 @@ int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, in
     if ((rc = conv(6, 8, 9, 0, 1, 1, 1, nullptr)) != FS_OK) return rc;
     if ((rc = conv(7, 9, 10, 0, 0, -1, 0, s->net.y)) != FS_OK) return rc;
     cnt.launches += 10;
-    if ((rc = fs_net_prolong(s->net.y, prev, s->pguess, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa,
-                             s->stream)) != FS_OK)
-        return rc;
-    CK(launch_learned_select(s->div, s->pguess, prev, s->rows, s->cols, s->pitch, s->net.res, s->net.counters,
-                             s->stream));
-    cnt.launches += 3;
+    // candidate A: the network's correction, post-smoothed; B: the coarse smoothing alone
+    float* pb = s->p[1];  // free between pressure passes
+    CK(launch_coarse_smooth(s->net.y, s->net.y, s->net.bs, s->net.scale, kNetKappa, kNetG, kCoarseSweeps, converged,
+                            s->stream));
+    CK(launch_coarse_smooth(nullptr, s->net.yc, s->net.bs, s->net.scale, kNetKappa, kNetG, kCoarseSweeps, converged,
+                            s->stream));
+    CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa, converged,
+                      s->stream));
+    CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa, converged,
+                      s->stream));
+    CK(cudaMemsetAsync(s->net.res + 1, 0, 2 * sizeof(double), s->stream));
+    CK(launch_energy_gain(s->div, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
+    CK(launch_energy_gain(s->div, p_cur, pb, s->rows, s->cols, s->pitch, s->net.res + 2, converged, s->stream));
+    CK(launch_accept_best(p_cur, s->pguess, pb, (long)s->field_floats, s->net.res + 1, converged, s->net.counters,
+                          s->stream));
+    cnt.launches += 9;
     return FS_OK;
+}
+
+// Starting pressure of a fixed-count projection with the learned warm start: the
+// previous pressure (zero on the first step) in pwarm[slot], corrected once.
+int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, int slot, Counter& cnt) {
+    int rc = enqueue_div_pass(s, u_in, v_in, cnt);
+    if (rc != FS_OK) return rc;
+    if (!s->warm_valid) CK(cudaMemsetAsync(s->pwarm[slot], 0, s->field_floats * sizeof(float), s->stream));
+    return enqueue_network_correction(s, s->pwarm[slot], nullptr, cnt);
 }
 
 // Starting pressure of projection `slot`: the network's guess, the previous pressure,
@@ -349,7 +381,7 @@ int projection_start(fs_solver* s, const float* u_in, const float* v_in, int slo
     if (s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready) {
         int rc = enqueue_learned_guess(s, u_in, v_in, slot, cnt);
         if (rc != FS_OK) return rc;
-        *pin = s->pguess;
+        *pin = s->pwarm[slot];
     }
     if (s->cfg.capture) {
         if (*pin)
@@ -373,8 +405,97 @@ int capture_div(fs_solver* s, int slot) {
 // Residual-driven projection: one persistent cooperative launch runs depth-K passes
 // until the relative residual ||div + sum(nbrs) - 4p|| / ||div|| is <= tol or the
 // iteration cap is reached, then the gradient subtract (see pressure_solve_kernel).
+int enqueue_fin_pass(fs_solver* s, const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                     Counter& cnt) {
+    StencilLaunch L{};
+    L.nfields = 1;
+    StencilField& f = L.f[0];
+    set_geometry(f, s, 1);
+    f.s_lr = f.s_tb = 1.f;
+    f.sweeps = 0;
+    f.h = grid_h(s->rows, s->cols);
+    f.kind = PASS_PRESSURE;
+    f.x = p;
+    f.cst = s->div;
+    f.y = nullptr;
+    f.epilogue = 1;
+    f.u_in = u_in;
+    f.v_in = v_in;
+    f.u_out = u_out;
+    f.v_out = v_out;
+    f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
+    PROF_BEGIN(s);
+    CK(launch_stencil(L, s->tile_rows, s->stream));
+    PROF_END(s, FS_KIND_STENCIL, interior_cells(s) * 28.0);  // read p, u, v (+div); write u, v
+    cnt.launches++;
+    cnt.passes++;
+    return FS_OK;
+}
+
+// Residual-driven projection with learned corrections: the current pressure starts
+// as the previous one (zero on the first step); each cycle corrects it with the network
+// (kept only if the coarse residual drops) and runs a segment of Jacobi passes until
+// the residual target or the segment's budget. Outside a stream capture the host reads
+// each segment's outcome and stops at convergence; inside one, all cycles are recorded
+// and those after convergence do nothing. Cycles: learned_cycles, or as many as the
+// iteration cap allows; the last gets the rest of the cap.
+int enqueue_project_learned_cycles(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                                   int slot, Counter& cnt) {
+    const int K = s->sweeps;
+    const int per = s->cfg.learned_cycle_iterations > 0 ? s->cfg.learned_cycle_iterations : 128;
+    const int cap = s->cfg.pressure_max_iterations;
+    const int cycles = s->cfg.learned_cycles > 0 ? s->cfg.learned_cycles : std::max(1, (cap + per - 1) / per);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s->stream, &capture));
+    const bool adaptive = capture == cudaStreamCaptureStatusNone && s->host_ctrl != nullptr;
+    int rc = enqueue_div_pass(s, u_in, v_in, cnt);
+    if (rc != FS_OK) return rc;
+    float* pcur = s->pwarm[slot];
+    if (!s->warm_valid) CK(cudaMemsetAsync(pcur, 0, s->field_floats * sizeof(float), s->stream));
+    if (s->cfg.capture)
+        CK(cudaMemcpyAsync(s->cap_start[slot], pcur, s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                           s->stream));
+    CK(cudaMemsetAsync(s->ctrl + slot, 0, sizeof(SolveCtrl), s->stream));
+    PressureSolve P{};
+    set_geometry(P.mid, s, K + 1);
+    P.mid.s_lr = P.mid.s_tb = 1.f;
+    P.mid.sweeps = K;
+    P.mid.h = grid_h(s->rows, s->cols);
+    P.mid.kind = PASS_PRESSURE;
+    P.mid.cst = s->div;
+    P.first = P.mid;
+    P.first.x = pcur;
+    P.p[0] = s->p[0];
+    P.p[1] = s->p[1];
+    P.partials = s->partials[slot];
+    P.ctrl = s->ctrl + slot;
+    P.tol = s->cfg.pressure_tolerance;
+    P.segment = 1;
+    P.p_cur = pcur;
+    const int blocks = std::min(s->solve_blocks, P.mid.tiles_x * P.mid.tiles_y);
+    for (int c = 0; c < cycles; ++c) {
+        if ((rc = enqueue_network_correction(s, pcur, &P.ctrl->converged, cnt)) != FS_OK) return rc;
+        const int budget = c + 1 < cycles ? per : std::max(per, cap - (cycles - 1) * per);
+        P.max_passes = std::max(1, (budget + K - 1) / K);
+        PROF_BEGIN(s);
+        CK(launch_pressure_solve(P, s->tile_rows, blocks, s->stream));
+        PROF_END(s, FS_KIND_STENCIL, 0.0);  // bytes depend on the iteration count reached
+        cnt.launches++;
+        cnt.passes++;
+        if (adaptive && c + 1 < cycles) {
+            CK(cudaMemcpyAsync(s->host_ctrl, P.ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s->stream));
+            CK(cudaStreamSynchronize(s->stream));
+            if (s->host_ctrl->converged || s->host_ctrl->error) break;
+        }
+    }
+    if ((rc = enqueue_fin_pass(s, pcur, u_in, v_in, u_out, v_out, cnt)) != FS_OK) return rc;
+    return capture_div(s, slot);
+}
+
 int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
                                 int slot, Counter& cnt) {
+    if (s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready)
+        return enqueue_project_learned_cycles(s, u_in, v_in, u_out, v_out, slot, cnt);
     const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
     const int K = s->sweeps;
@@ -548,7 +669,9 @@ int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
     const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     for (int k = 0; k < nsteps; ++k) {
         // The first warm-start step starts from zero pressure; its graph differs.
-        bool graphable = s->cfg.use_graph && (!warm || s->warm_valid);
+        // learned corrections to a residual target stop at convergence, read on the host
+        const bool adaptive = s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready && s->cfg.pressure_tolerance > 0.f;
+        bool graphable = s->cfg.use_graph && (!warm || s->warm_valid) && !adaptive;
         if (graphable && (!s->graph_valid || diff != s->g_diff || visc != s->g_visc || dt != s->g_dt)) {
             destroy_graph(s);
             Counter cnt;
@@ -783,7 +906,7 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         size_t acts = 0;
         for (int k = 0; k < kNetActs; ++k) acts += net_act_pixels(k) * kNetC;
         const size_t bytes = (size_t)FS_NET_PARAMS * 4 + 8 * 9216 * 2 + acts * 2 + (size_t)kNetG * kNetG * kNetC * 4 +
-                             256 * 4;
+                             256 * 4 + 2 * (size_t)kNetG * kNetG * 4 + (size_t)kNetG * kNetG * kNetC * 4;
         if ((e = cudaMalloc(&s->net.mem, bytes)) != cudaSuccess || (e = cudaMemset(s->net.mem, 0, bytes)) != cudaSuccess) {
             rc = cuda_fail(e, "fs_create: network buffers");
         } else {
@@ -796,13 +919,18 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
             q += acts * 2;
             s->net.y = reinterpret_cast<float*>(q);
             q += (size_t)kNetG * kNetG * kNetC * 4;
-            s->net.res = reinterpret_cast<double*>(q);
-            s->net.counters = reinterpret_cast<unsigned long long*>(q + 16);
-            s->net.scale = reinterpret_cast<float*>(q + 32);
-            s->net.err = reinterpret_cast<int*>(q + 36);
+            s->net.res = reinterpret_cast<double*>(q);                          // 4 doubles
+            s->net.counters = reinterpret_cast<unsigned long long*>(q + 32);    // 2
+            s->net.scale = reinterpret_cast<float*>(q + 48);
+            s->net.err = reinterpret_cast<int*>(q + 52);
+            s->net.bs = reinterpret_cast<float*>(q + 256 * 4);
+            s->net.yc = s->net.bs + 2 * (size_t)kNetG * kNetG;
         }
     }
+    if (rc == FS_OK && learned && (e = cudaMallocHost(&s->host_ctrl, sizeof(SolveCtrl))) != cudaSuccess)
+        rc = cuda_fail(e, "fs_create: pinned control block");
     if (rc != FS_OK) {
+        if (s->host_ctrl) cudaFreeHost(s->host_ctrl);
         if (s->net.mem) cudaFree(s->net.mem);
         if (s->stream) cudaStreamDestroy(s->stream);
         cudaFree(s->slab);
@@ -828,6 +956,7 @@ int fs_destroy(fs_solver* s) {
     destroy_graph(s);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->net.mem) cudaFree(s->net.mem);
+    if (s->host_ctrl) cudaFreeHost(s->host_ctrl);
     cudaFree(s->slab);
     delete s;
     return FS_OK;

@@ -426,15 +426,21 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     const int ntiles = P.mid.tiles_x * P.mid.tiles_y;
     int passes = 0;
     double ratio = 0.0;
-    bool ok = true;
+    bool ok = true, done = false;
+    int cur = -1;  // index in P.p of the latest pressure; -1 before the first pass
+    // segment mode, converged in an earlier segment: the flag was written by an earlier
+    // launch, so every CTA reads the same value and none waits at a barrier
+    if (P.segment && __ldcg(&P.ctrl->converged)) return;
+    int pass = 0;
 #pragma unroll 1
-    for (int pass = 0; pass < P.max_passes; ++pass) {
-        const StencilField& F = pass == 0 ? P.first : P.mid;
-        const float* x = pass == 0 ? F.x : P.p[(pass - 1) & 1];
+    for (; ok && !done && pass < P.max_passes; ++pass) {
+        const StencilField& F = cur < 0 ? P.first : P.mid;
+        const float* x = cur < 0 ? F.x : P.p[cur];
+        const int dst = cur < 0 ? 0 : cur ^ 1;
         float rn = 0.f, rd = 0.f;
 #pragma unroll 1
         for (int t = blockIdx.x; t < ntiles; t += G)
-            pressure_tile<TY, SR>(F, t, x, P.p[pass & 1], true, rn, rd);
+            pressure_tile<TY, SR>(F, t, x, P.p[dst], true, rn, rd);
         double a = rn, b = rd;
         block_sum2(a, b);
         double* part = P.partials + (size_t)(pass & 1) * 2 * G;
@@ -443,7 +449,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             part[2 * blockIdx.x + 1] = b;
         }
         ok = grid_barrier(P.ctrl, G);
-        passes = pass + 1;
+        passes++;
+        cur = dst;
         if (!ok) break;
         // every CTA sums all partials in the same order, so all agree on the outcome
         a = 0.0;
@@ -454,19 +461,26 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
         }
         block_sum2(a, b);
         ratio = b > 0.0 ? sqrt(a / b) : sqrt(a);
-        if (ratio <= (double)P.tol) break;
+        done = ratio <= (double)P.tol;
     }
-    if (ok) {
-        // gradient subtract + reflecting fills from the final pressure
-        const int nfin = P.fin.tiles_x * P.fin.tiles_y;
-        const float* pf = P.p[(passes - 1) & 1];
-        float rn = 0.f, rd = 0.f;
+    if (ok && cur >= 0) {
+        if (P.segment) {
+            // every CTA passed the last pass's barrier: the final pressure is complete
+            const float4* src = reinterpret_cast<const float4*>(P.p[cur]);
+            float4* dst = reinterpret_cast<float4*>(P.p_cur);
+            const long n4 = (long)P.mid.rows * P.mid.pitch / 4;
+            for (long e = (long)blockIdx.x * nt + tid; e < n4; e += (long)G * nt) dst[e] = __ldcg(src + e);
+        } else {
+            // gradient subtract + reflecting fills from the final pressure
+            const int nfin = P.fin.tiles_x * P.fin.tiles_y;
+            float rn = 0.f, rd = 0.f;
 #pragma unroll 1
-        for (int t = blockIdx.x; t < nfin; t += G)
-            pressure_tile<TY, SR>(P.fin, t, pf, P.p_out, false, rn, rd);
+            for (int t = blockIdx.x; t < nfin; t += G)
+                pressure_tile<TY, SR>(P.fin, t, P.p[cur], P.p_out, false, rn, rd);
+        }
     }
     if (blockIdx.x == 0 && tid == 0) {
-        P.ctrl->passes = passes;
+        P.ctrl->passes = (P.segment ? P.ctrl->passes : 0) + passes;
         P.ctrl->residual = ratio;
         P.ctrl->converged = ok && ratio <= (double)P.tol;
     }

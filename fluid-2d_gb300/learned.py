@@ -1,17 +1,22 @@
-"""Learned warm start for the pressure solve: a small convolutional network that maps
-the divergence and the previous pressure to a pressure correction.
+"""Learned pressure correction: a small convolutional network that maps the residual of
+the current pressure (the divergence and the previous pressure combined) to a correction.
 
 No counterpart in the reference (its pressure solve always starts from zero,
-src/fluid_solver_gpu.cu:364). The network runs on a fixed coarse grid of G x G cells
-(G = 32), each covering an R x R block of the fine interior: its input is the block
-SUM of the divergence (channel 0, divided by the RMS of those sums, `scale`) and the
-block MEAN of the previous pressure (channel 1, divided by scale * KAPPA); its output
-(channel 0, times scale * KAPPA) is the correction of the block mean pressure,
-interpolated bilinearly back to the fine grid and added to the previous pressure. The
-coarse problem (block sums of the divergence) has the same units as the fine one, so
-one network serves every fine size that G divides. Jacobi then runs from that guess;
-the solver keeps the plain previous pressure instead whenever the guess has the larger
-residual.
+src/fluid_solver_gpu.cu:364). The network runs on a coarse grid of G x G cells (G = 32),
+each covering an R x R block of the fine interior: its input (channel 0) is the block
+SUM of the Poisson residual r = div + sum(nbrs p) - 4p of the current pressure p,
+divided by the RMS of those sums (`scale`); when p is the previous step's pressure this
+is the divergence and the previous pressure in one field, and when p is zero it is the
+block-summed divergence. Its output (channel 0, times scale * KAPPA) is the block mean
+of the correction e that solves the residual equation (4e - sum(nbrs e) = r), which is
+interpolated bilinearly back to the fine grid and added to p. The coarse problem has the
+same units at every fine size that G divides, so one network serves them all.
+
+In a fixed-count solve the network corrects the previous pressure once and the solver
+keeps whichever of the two starts has the lower residual. In a solve to a residual
+target the network corrects the current pressure before each segment of Jacobi
+sweeps, and the segment's first pass runs from both the corrected and the uncorrected
+pressure and keeps the better, so a correction that does not help costs one pass.
 
 Architecture (8 conv layers, 3x3, 32 channels, BF16 operands, FP32 accumulation; two
 average-pool downsamples and two nearest upsamples with additive skips):

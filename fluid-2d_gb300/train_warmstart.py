@@ -1,13 +1,16 @@
-"""Training data and training loop for the learned pressure warm start.
+"""Training data and training loop for the learned pressure correction.
 
 Data: seeded random-vortex runs of the solver itself (previous-pressure warm start,
-capture on). For every projection the solver keeps the divergence it projected and the
-pressure it started from; the exact solution p* of the same discrete Neumann problem
-(4p - sum of neighbours = div on the interior, edges equal to their inner neighbour) is
-computed in FP64 with the discrete cosine transform that diagonalises it, and the
-training target is the block-mean correction p*_c - p_start_c on the coarse grid, zero
-mean, in network units. Inputs come from the same restriction kernel the solver runs at
-inference (fs_net_restrict), so training and inference see identical preprocessing.
+fixed sweep counts, capture on). For every projection the solver keeps the divergence
+it projected, the pressure it started from and the pressure it ended with; each of the
+two pressures gives one sample, so the data holds both the residuals the network sees
+first in a step (of the previous step's pressure) and those it sees after a segment of
+Jacobi sweeps. The exact solution p* of the same discrete Neumann problem (4p - sum of
+neighbours = div on the interior, edges equal to their inner neighbour) is computed in
+FP64 with the discrete cosine transform that diagonalises it; the training target is
+the block-mean correction p*_c - p_c on the coarse grid, zero mean, in network units.
+Inputs come from the same restriction kernel the solver runs (fs_net_restrict), so
+training and inference see identical preprocessing.
 
 Training: Adam on mean squared error, forward and backward on the project's kernels
 (learned.Net). torch supplies device buffers and the FP64 DCT matrices only.
@@ -67,8 +70,9 @@ def _view(ptr, rows, pitch, device):
     return out
 
 
-def generate(n_samples, size=512, steps_per_run=100, seed=100, kp=40, device="cuda", log=None):
-    """Returns (X [S, G, G, 32] BF16 network inputs, T [S, G, G] FP32 targets, info)."""
+def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 1024), device="cuda", log=None):
+    """Returns (X [S, G, G, 32] BF16 network inputs, T [S, G, G] FP32 targets, info).
+    Run k uses sweeps[k % len(sweeps)] pressure sweeps per projection."""
     torch = _torch()
     import fluid2d_gb300 as pkg
     from fluid2d_gb300 import workloads
@@ -78,9 +82,11 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, kp=40, device="cu
     R = size // G
     xs, ts = [], []
     scale = torch.zeros(1, dtype=torch.float32, device=device)
+    work = torch.zeros(G * G, dtype=torch.float32, device=device)
     run = 0
     t0 = time.time()
     while len(ts) < n_samples:
+        kp = sweeps[run % len(sweeps)]
         w = workloads.vortex_field(size, seed=seed + run, kd=20, kp=kp, dt=0.05, rate=1e-5, vortices=16,
                                    rmin=size / 100.0, rmax=size / 25.0)
         s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=kp, warm_start=pkg.FS_WARM_PREVIOUS,
@@ -91,21 +97,21 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, kp=40, device="cu
         for _ in range(steps_per_run):
             s.step(w.diffusion, w.viscosity, w.dt, 1)
             for slot in (0, 1):
-                dptr, sptr, _ = s.capture_view(slot)
-                xin = torch.zeros((G, G, 32), dtype=torch.bfloat16, device=device)
-                pc = torch.zeros((G, G), dtype=torch.float32, device=device)
-                rc = L.fs_net_restrict(C.c_void_p(dptr), C.c_void_p(sptr), w.rows, w.cols, pitch, G, Lm.KAPPA,
-                                       C.c_void_p(scale.data_ptr()), C.c_void_p(xin.data_ptr()),
-                                       C.c_void_p(pc.data_ptr()), None)
-                if rc != 0:
-                    raise RuntimeError(L.fs_last_error().decode())
+                dptr, sptr, fptr = s.capture_view(slot)
                 div = _view(dptr, w.rows, pitch, device)[1:-1, 1:size + 1].double()
-                pstar = neumann_solve(div, Cm, lam)
-                pstar_c = pstar.reshape(G, R, G, R).mean(dim=(1, 3)).float()
-                corr = pstar_c - pc
-                corr = corr - corr.mean()
-                xs.append(xin)
-                ts.append(corr / (scale * Lm.KAPPA))
+                pstar_c = neumann_solve(div, Cm, lam).reshape(G, R, G, R).mean(dim=(1, 3)).float()
+                for pptr in (sptr, fptr):
+                    xin = torch.zeros((G, G, 32), dtype=torch.bfloat16, device=device)
+                    pc = torch.zeros((G, G), dtype=torch.float32, device=device)
+                    rc = L.fs_net_restrict(C.c_void_p(dptr), C.c_void_p(pptr), w.rows, w.cols, pitch, G,
+                                           C.c_void_p(work.data_ptr()), C.c_void_p(scale.data_ptr()),
+                                           C.c_void_p(xin.data_ptr()), C.c_void_p(pc.data_ptr()), None)
+                    if rc != 0:
+                        raise RuntimeError(L.fs_last_error().decode())
+                    corr = pstar_c - pc
+                    corr = corr - corr.mean()
+                    xs.append(xin)
+                    ts.append(corr / (scale * Lm.KAPPA))
                 if len(ts) >= n_samples:
                     break
             if len(ts) >= n_samples:
@@ -114,9 +120,9 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, kp=40, device="cu
         run += 1
         if log:
             log(f"generated {len(ts)} samples ({run} runs, {time.time() - t0:.1f} s)")
-    X = torch.stack(xs)
-    T = torch.stack(ts)
-    return X, T, {"runs": run, "size": size, "seconds": time.time() - t0}
+    X = torch.stack(xs[:n_samples])
+    T = torch.stack(ts[:n_samples])
+    return X, T, {"runs": run, "size": size, "seconds": time.time() - t0, "sweeps": list(sweeps)}
 
 
 def train(X, T, epochs=4, batch=128, lr=1e-3, seed=0, log=None):

@@ -50,7 +50,9 @@ extern "C" {
  * p_buffer.clear(0), src/fluid_solver_gpu.cu:364). */
 #define FS_WARM_ZERO 0
 #define FS_WARM_PREVIOUS 1
-#define FS_WARM_LEARNED 2 /* network correction of the previous pressure (fs_set_network) */
+#define FS_WARM_LEARNED 2 /* network corrections of the pressure (fs_set_network): of the previous
+                            pressure with a fixed sweep count; with a residual target, of the
+                            current pressure every learned_cycle_iterations sweeps */
 
 /* Solution method of the step. FS_METHOD_JACOBI is the reference's CUDA solver
  * (fluid_solver_gpu, src/fluid_solver_gpu.cu:209-404). FS_METHOD_GAUSS_SEIDEL reproduces
@@ -81,6 +83,11 @@ typedef struct fs_config {
     int capture;               /* 1: keep each projection's divergence and starting pressure
                                   for fs_capture_view (training-data generation) */
     int method;                /* FS_METHOD_JACOBI (default) or FS_METHOD_GAUSS_SEIDEL */
+    int learned_cycles;        /* FS_WARM_LEARNED with a residual target: most network
+                                  corrections per projection, each followed by Jacobi sweeps;
+                                  0 = as many as pressure_max_iterations allows. Steps stop at
+                                  convergence (read on the host after each segment). */
+    int learned_cycle_iterations; /* Jacobi sweeps after each correction; 0 = 128 */
 } fs_config;
 
 typedef struct fs_stats {
@@ -93,8 +100,8 @@ typedef struct fs_stats {
     int pressure_iterations_last[2]; /* sweeps used by the two projections of the last step */
     double pressure_residual_last[2];/* their final relative residuals (residual mode only) */
     int nonfinite;                   /* 1 if a NaN/Inf was flagged since the last check */
-    long long learned_used;          /* projections that started from the network's guess */
-    long long learned_fallback;      /* projections that kept the previous pressure instead */
+    long long learned_used;          /* network corrections kept (they lowered the residual) */
+    long long learned_fallback;      /* corrections rejected: the uncorrected pressure was better */
 } fs_stats;
 
 /* Device view of the resident state, for zero-copy use by other CUDA code. Each field
@@ -284,7 +291,10 @@ FS_API int fs_conv3x3(const void* x, const void* wpk, const float* w32, const fl
  *   cores, FP32 atomics); flip_weights: weights of the backward-data convolution;
  *   mse: loss on channel 0 and its gradient (per-CTA partial sums of squared error);
  *   adam: one Adam step on FP32 weights (frozen mask nullable);
- *   restrict / prolong: fine pitched fields <-> the G x G network grid (see net.cu). */
+ *   restrict: block sums of the Poisson residual of p_prev (null = zero) over the G x G
+ *   network grid into work (G*G floats), their RMS into *scale, network input channel 0 =
+ *   sums / scale (BF16, G*G*32), optional block means of p_prev into pc;
+ *   prolong: p_out = p_prev + bilinear interpolation of channel 0 of y times scale*kappa. */
 FS_API int fs_net_avgpool2(const void* x, void* y, int rows_out, int w_out, void* stream);
 FS_API int fs_net_avgpool2_bwd(const float* dy, float* dx, int rows_in, int w_in, void* stream);
 FS_API int fs_net_upsample2_bwd(const float* dup, float* dlow, int rows_low, int w_low, void* stream);
@@ -296,7 +306,7 @@ FS_API int fs_net_flip_weights(const float* w, float* wt, void* stream);
 FS_API int fs_net_mse(const float* y, const float* target, float* dy, float* loss_part, long long n, void* stream);
 FS_API int fs_net_adam(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
                        float eps, int step, const unsigned char* frozen, void* stream);
-FS_API int fs_net_restrict(const float* div, const float* p_prev, int rows, int cols, int pitch, int G, float kappa,
+FS_API int fs_net_restrict(const float* div, const float* p_prev, int rows, int cols, int pitch, int G, float* work,
                            float* scale, void* xin, float* pc, void* stream);
 FS_API int fs_net_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
                           const float* scale, float kappa, void* stream);

@@ -1,12 +1,15 @@
 """The learned pressure warm start: network forward and gradients (tensor-core convs and
 CUDA-core weight gradients) against a CPU reference, the exact Neumann solver used for
 training targets against the oracle's Jacobi, training, and the solver's learned mode."""
+import pathlib
+
 import numpy as np
 import pytest
 
 import oracle
 
 pytestmark = pytest.mark.gpu
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
 
 
 def _mods():
@@ -109,3 +112,85 @@ def test_learned_mode_keeps_parity_from_the_start_it_used(fluid, wl):
                 assert oracle.rel_linf(g_, o) <= 1e-5
         st = s.stats()
         assert st["learned_used"] + st["learned_fallback"] == 8
+
+
+def _field(fluid, ptr, rows, cols, pitch):
+    from fluid2d_gb300 import train_warmstart as T
+
+    return np.ascontiguousarray(T._view(ptr, rows, pitch, "cuda")[:, :cols].cpu().numpy())
+
+
+@pytest.mark.parametrize("trained", [False, True])
+def test_learned_cycles_reach_the_target_and_keep_parity(fluid, wl, trained):
+    """Residual-target projections with network corrections: every projection meets the
+    target (the residual of the pressure it ended with, recomputed by the oracle), and
+    the step equals the oracle's step that projects with those final pressures. With
+    untrained weights the judge rejects the corrections and the solve still converges."""
+    Lm, T = _mods()
+    if trained:
+        X, Y, _ = T.generate(512, size=128, steps_per_run=32, seed=21, sweeps=(32, 128))
+        params, _ = T.train(X, Y, epochs=6, batch=64, lr=2e-3, seed=0)
+    else:
+        params = Lm.init_params(1)
+    w = wl.vortex_field(128, seed=5, kd=15, kp=20, dt=0.1, rate=1e-3, vortices=6, rmin=4, rmax=12)
+    d, u, v = w.state()
+    tol = 2e-2
+    with fluid.Solver(w.rows, w.cols, warm_start=fluid.FS_WARM_LEARNED, capture=1, device=0,
+                      pressure_tolerance=tol, pressure_max_iterations=60000, learned_cycles=3,
+                      learned_cycle_iterations=64) as s:
+        s.set_network(params)
+        pitch = s.device_view().pitch
+        for _ in range(3):
+            od, ou, ov = d.copy(), u.copy(), v.copy()
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            st = s.stats()
+            assert max(st["pressure_residual_last"]) <= tol
+            finals = []
+            for slot in (0, 1):
+                dptr, _, fptr = s.capture_view(slot)
+                pf = _field(fluid, fptr, w.rows, w.cols, pitch)
+                dv = _field(fluid, dptr, w.rows, w.cols, pitch)
+                assert oracle.residual(pf, dv) <= tol * 1.001
+                finals.append(pf)
+            od, ou, ov = oracle.gpu_solve_ex(od, w.ds, w.diffusion, ou, ov, w.us, w.vs, w.viscosity, w.dt, 15, 0, 0,
+                                             pw=[finals[0].copy(), finals[1].copy()])
+            for g_, o in ((d, od), (u, ou), (v, ov)):
+                assert oracle.rel_linf(g_, o) <= 1e-5
+        st = s.stats()
+        assert st["learned_used"] + st["learned_fallback"] >= 6
+        if trained:
+            assert st["learned_used"] >= 1
+
+
+def _sweeps(fluid, w, warm, params, tol, steps=3, cap=20000):
+    total = 0
+    with fluid.Solver(w.rows, w.cols, diffuse_iterations=20, warm_start=warm, device=0, check_finite=0,
+                      pressure_tolerance=tol, pressure_max_iterations=cap) as s:
+        if params is not None:
+            s.set_network(params)
+        s.upload(*w.state())
+        s.upload_sources(*w.sources())
+        for _ in range(steps):
+            s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False)
+            try:
+                s.sync()
+            except fluid.FluidError as e:
+                if e.code != fluid.FS_ERR_NOT_CONVERGED:
+                    raise
+            total += sum(s.stats()["pressure_iterations_last"])
+    return total
+
+
+def test_trained_network_cuts_sweeps(fluid, wl):
+    """What the trained network gains: the committed parameters (trained on the GPU by
+    `bench.py --workload learned --samples 20000 --epochs 12 --weights ...` on 512^2
+    runs) against the previous-pressure warm start and against an all-zero network
+    (coarse post-smoothing alone), on a 258^2 vortex field solved to a 5e-2 residual."""
+    params = np.load(GOLDEN / "warmstart_params.npy").astype(np.float32)
+    w = wl.vortex_field(256, seed=8, kd=20, kp=20, dt=0.05, rate=1e-5, vortices=32, rmin=5, rmax=20)
+    prev = _sweeps(fluid, w, fluid.FS_WARM_PREVIOUS, None, 5e-2)
+    learned = _sweeps(fluid, w, fluid.FS_WARM_LEARNED, params, 5e-2)
+    coarse = _sweeps(fluid, w, fluid.FS_WARM_LEARNED, np.zeros_like(params), 5e-2)
+    print(f"sweeps over 3 steps: previous {prev}, learned {learned}, coarse smoothing only {coarse}")
+    assert learned <= 0.5 * prev
+    assert learned <= coarse
