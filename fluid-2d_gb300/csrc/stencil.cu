@@ -75,23 +75,29 @@ __device__ __forceinline__ void run_sweeps(const float (&k)[SR], int& co, int& n
     constexpr int RW = kRegionW;
     extern __shared__ float4 smem4[];
     float* const S = reinterpret_cast<float*>(smem4);
-    const int rup = r0 > 0 ? r0 - 1 : 0;
-    const int rlast = (r0 + SR < RH) ? r0 + SR : r0 + SR - 1;
+    // offsets from this thread's first cell: the row above (clamped at the region top),
+    // the row below the last (clamped at the bottom), the left and right neighbours
+    // (clamped at the region sides); the clamped cells compute values nothing uses
+    const int up_off = r0 > 0 ? -RW : 0;
+    const int dn_off = (r0 + SR < RH) ? SR * RW : (SR - 1) * RW;
+    const int l_off = txl - tx, r_off = txr - tx;
+    const int base = r0 * RW + tx;
 #pragma unroll 1
     for (int s = 0; s < nsweeps; ++s) {
-        const float* __restrict__ cr = S + co;
-        float* __restrict__ nx = S + no;
-        float up = cr[rup * RW + tx];
-        float ce = cr[r0 * RW + tx];
+        const float* __restrict__ c = S + co + base;
+        const float* __restrict__ cl = c + l_off;
+        const float* __restrict__ cr = c + r_off;
+        float* __restrict__ nx = S + no + base;
+        float up = c[up_off];
+        float ce = c[0];
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i;
-            const float dn = cr[(i + 1 < SR ? r + 1 : rlast) * RW + tx];
-            const float Lv = cr[r * RW + txl], Rv = cr[r * RW + txr];
+            const float dn = i + 1 < SR ? c[(i + 1) * RW] : c[dn_off];
+            const float Lv = cl[i * RW], Rv = cr[i * RW];
             float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, dn, a, dh, dl, rf)
                             : pressure_update(k[i], Lv, Rv, up, dn);
             if (EDGE) nv = ((live >> i) & 1u) ? nv : ce;
-            nx[r * RW + tx] = nv;
+            nx[i * RW] = nv;
             up = ce;
             ce = dn;
         }
@@ -111,7 +117,7 @@ __device__ __forceinline__ void run_sweeps(const float (&k)[SR], int& co, int& n
                     else if (gc == cols - 1) src = r * RW + txl;
                     sg = s_lr;
                 }
-                if (src >= 0) nx[r * RW + tx] = sg * nx[src];
+                if (src >= 0) S[no + r * RW + tx] = sg * S[no + src];
             }
             __syncthreads();
         }
@@ -151,31 +157,45 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 
     float c[SR], k[SR];
 
+    // Row masks of this thread's column segment (bit i = row r0 + i of the region),
+    // computed once so that the unrolled row loops below test one bit per row:
+    //   m_in  - the cell lies in the grid (loads);
+    //   m_int - the cell is an interior cell (constant terms, add_sources, live cells);
+    //   m_out - the cell is in this tile's output and in the grid (stores).
+    const int g0 = gy0 + r0;  // grid row of bit 0
+    auto range = [](int lo, int hi) -> unsigned {
+        lo = max(lo, 0);
+        hi = min(hi, SR);
+        return hi > lo ? (((hi - lo) >= 32 ? ~0u : ((1u << (hi - lo)) - 1u)) << lo) : 0u;
+    };
+    const unsigned m_in = col_in ? range(-g0, rows - g0) : 0u;
+    const unsigned m_int = col_int ? range(1 - g0, rows - 1 - g0) : 0u;
+    const size_t o0 = (size_t)((long long)g0 * (long long)pitch + gc);  // offset of bit 0 (wraps if g0 < 0;
+                                                                         // only masked rows are dereferenced)
+
     // ------------------------------------------------------------------ load
     if (kind == PASS_PRESSURE_FIRST) {
         // divergence_kernel (fluid_solver_gpu.cu:173-174) on the region, from u, v
         // staged in the two shared buffers.
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const int gr = gy0 + r0 + i;
-            const bool in = col_in && gr >= 0 && gr < rows;
-            const size_t o = (size_t)gr * pitch + gc;
+            const bool in = (m_in >> i) & 1u;
+            const size_t o = o0 + (size_t)i * pitch;
             S[co + (r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
             S[no + (r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
         }
         __syncthreads();
         const float cdiv = F.cdiv;
+        const float* __restrict__ cst = F.cst;
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i, gr = gy0 + r;
+            const int r = r0 + i;
             const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
             float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
             s = __fadd_rn(s, S[no + rd * RW + tx]);
             s = __fsub_rn(s, S[no + ru * RW + tx]);
-            const bool interior = col_int && gr >= 1 && gr <= rows - 2;
-            k[i] = interior ? __fmul_rn(cdiv, s) : 0.f;
-            const bool in = col_in && gr >= 0 && gr < rows;
-            c[i] = (F.cst != nullptr && in) ? __ldcg(F.cst + (size_t)gr * pitch + gc) : 0.f;
+            k[i] = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
+            c[i] = (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
         }
         __syncthreads();
     } else if (kind == PASS_DIFFUSE_FIRST) {
@@ -183,24 +203,18 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         const float dt = F.dt;
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const int gr = gy0 + r0 + i;
-            const bool in = col_in && gr >= 0 && gr < rows;
-            const bool interior = col_int && gr >= 1 && gr <= rows - 2;
-            const size_t o = (size_t)gr * pitch + gc;
-            float x = in ? __ldcg(xin + o) : 0.f;
-            if (interior) x = __fadd_rn(x, __fmul_rn(dt, __ldcg(F.x2 + o)));
+            const size_t o = o0 + (size_t)i * pitch;
+            float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
+            if ((m_int >> i) & 1u) x = __fadd_rn(x, __fmul_rn(dt, __ldcg(F.x2 + o)));
             c[i] = x;
             k[i] = x;
         }
     } else {
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
-            const int gr = gy0 + r0 + i;
-            const bool in = col_in && gr >= 0 && gr < rows;
-            const bool interior = col_int && gr >= 1 && gr <= rows - 2;
-            const size_t o = (size_t)gr * pitch + gc;
-            c[i] = in ? __ldcg(xin + o) : 0.f;
-            k[i] = interior ? __ldcg(F.cst + o) : 0.f;
+            const size_t o = o0 + (size_t)i * pitch;
+            c[i] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
+            k[i] = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
         }
     }
 #pragma unroll
@@ -210,13 +224,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // ------------------------------------------------------------------ sweeps
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
     if (edge_cta) {
-        unsigned live = 0;
-#pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const int gr = gy0 + r0 + i;
-            live |= (unsigned)(col_int && gr >= 1 && gr <= rows - 2) << i;
-        }
-        run_sweeps<DIFF, true, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, live, gy0, gc, rows, cols, F.s_lr,
+        run_sweeps<DIFF, true, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, m_int, gy0, gc, rows, cols, F.s_lr,
                                        F.s_tb, F.a, F.dh, F.dl, F.rf);
     } else {
         run_sweeps<DIFF, false, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
@@ -228,14 +236,19 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 
     // ------------------------------------------------------------------ store
     const bool col_out = col_in && tx >= H && tx < H + F.tile_w;
-    if (col_out) {
+    const unsigned m_out = col_out ? (range(H - r0, H + F.tile_h - r0) & m_in) : 0u;
+    if (m_out) {
+        float* __restrict__ y = yout;
+        float* __restrict__ ko = F.cst_out;
+        if (y) {
 #pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i, gr = gy0 + r;
-            if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
-            const size_t o = (size_t)gr * pitch + gc;
-            if (yout) yout[o] = c[i];
-            if (F.cst_out) F.cst_out[o] = k[i];
+            for (int i = 0; i < SR; ++i)
+                if ((m_out >> i) & 1u) y[o0 + (size_t)i * pitch] = c[i];
+        }
+        if (ko) {
+#pragma unroll
+            for (int i = 0; i < SR; ++i)
+                if ((m_out >> i) & 1u) ko[o0 + (size_t)i * pitch] = k[i];
         }
     }
     if (F.epilogue && col_out) {
