@@ -55,6 +55,31 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
     return __fmul_rn(s, 0.25f);
 }
 
+// The same updates on two cells at once with the packed FP32 pipe (sm_100+): each lane
+// of a float2 rounds exactly as the scalar form, so results are bit-identical; -q*dh is
+// written q*(-dh), the same exact product.
+__device__ __forceinline__ float2 diffuse_update2(float2 x0, float2 L, float2 R, float2 U, float2 D, float2 a,
+                                                  float2 ndh, float2 ndl, float2 rf) {
+    float2 s = __fadd2_rn(L, R);
+    s = __fadd2_rn(s, U);
+    s = __fadd2_rn(s, D);
+    // x0 + a*s with two roundings, as the reference: formed lane by lane, because the
+    // compiler may fuse a packed multiply feeding a packed add into one FFMA2
+    const float2 num = make_float2(__fadd_rn(x0.x, __fmul_rn(a.x, s.x)), __fadd_rn(x0.y, __fmul_rn(a.y, s.y)));
+    const float2 q = __fmul2_rn(num, rf);
+    float2 e = __ffma2_rn(q, ndh, num);
+    e = __ffma2_rn(q, ndl, e);
+    return __ffma2_rn(e, rf, q);
+}
+
+__device__ __forceinline__ float2 pressure_update2(float2 dv, float2 L, float2 R, float2 U, float2 D) {
+    float2 s = __fadd2_rn(dv, R);
+    s = __fadd2_rn(s, L);
+    s = __fadd2_rn(s, D);
+    s = __fadd2_rn(s, U);
+    return __fmul2_rn(s, make_float2(0.25f, 0.25f));
+}
+
 // All sweeps of one tile. Each thread owns one column of SR rows of the region and
 // keeps only its constant term (x0 or div) in registers: every sweep streams down the
 // column with a rolling up/centre/down window read from `cur` (the previous sweep) plus
@@ -68,11 +93,11 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
 //                 each sweep the domain-edge cells take their inner neighbour's new value
 //                 (set_boundary_*, fluid_solver_gpu.cu:11-54); corners keep theirs.
 template <bool DIFF, bool EDGE, int SR, int RH>
-__device__ __forceinline__ void run_sweeps(const float (&k)[SR], int& co, int& no, int nsweeps, int r0,
+__device__ __forceinline__ void run_sweeps(const float2 (&k2)[SR / 2], int& co, int& no, int nsweeps, int r0,
                                            int tx, int txl, int txr, unsigned live, int gy0, int gc, int rows,
                                            int cols, float s_lr, float s_tb, float a, float dh, float dl,
                                            float rf) {
-    constexpr int RW = kRegionW;
+    constexpr int RW = kRegionW, H2 = SR / 2;
     extern __shared__ float4 smem4[];
     float* const S = reinterpret_cast<float*>(smem4);
     // offsets from this thread's first cell: the row above (clamped at the region top),
@@ -82,22 +107,30 @@ __device__ __forceinline__ void run_sweeps(const float (&k)[SR], int& co, int& n
     const int dn_off = (r0 + SR < RH) ? SR * RW : (SR - 1) * RW;
     const int l_off = txl - tx, r_off = txr - tx;
     const int base = r0 * RW + tx;
+    const float2 a2 = make_float2(a, a), ndh2 = make_float2(-dh, -dh), ndl2 = make_float2(-dl, -dl);
+    const float2 rf2 = make_float2(rf, rf);
 #pragma unroll 1
     for (int s = 0; s < nsweeps; ++s) {
         const float* __restrict__ c = S + co + base;
         const float* __restrict__ cl = c + l_off;
         const float* __restrict__ cr = c + r_off;
         float* __restrict__ nx = S + no + base;
-        float up = c[up_off];
-        float ce = c[0];
+        // two rolling windows down the segment in lockstep: rows j (x) and j + SR/2 (y)
+        float2 up = make_float2(c[up_off], c[(H2 - 1) * RW]);
+        float2 ce = make_float2(c[0], c[H2 * RW]);
 #pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const float dn = i + 1 < SR ? c[(i + 1) * RW] : c[dn_off];
-            const float Lv = cl[i * RW], Rv = cr[i * RW];
-            float nv = DIFF ? diffuse_update(k[i], Lv, Rv, up, dn, a, dh, dl, rf)
-                            : pressure_update(k[i], Lv, Rv, up, dn);
-            if (EDGE) nv = ((live >> i) & 1u) ? nv : ce;
-            nx[i * RW] = nv;
+        for (int j = 0; j < H2; ++j) {
+            const float2 dn = make_float2(c[(j + 1) * RW], j + 1 + H2 < SR ? c[(j + 1 + H2) * RW] : c[dn_off]);
+            const float2 Lv = make_float2(cl[j * RW], cl[(j + H2) * RW]);
+            const float2 Rv = make_float2(cr[j * RW], cr[(j + H2) * RW]);
+            float2 nv = DIFF ? diffuse_update2(k2[j], Lv, Rv, up, dn, a2, ndh2, ndl2, rf2)
+                             : pressure_update2(k2[j], Lv, Rv, up, dn);
+            if (EDGE) {
+                nv.x = ((live >> j) & 1u) ? nv.x : ce.x;
+                nv.y = ((live >> (j + H2)) & 1u) ? nv.y : ce.y;
+            }
+            nx[j * RW] = nv.x;
+            nx[(j + H2) * RW] = nv.y;
             up = ce;
             ce = dn;
         }
@@ -155,7 +188,9 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txl = tx > 0 ? tx - 1 : 0;
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
 
-    float c[SR], k[SR];
+    float c[SR];
+    float2 k2[SR / 2];  // constant terms: row i in k2[i].x (i < SR/2) or k2[i - SR/2].y
+#define KREF(i) ((i) < SR / 2 ? k2[(i)].x : k2[(i) - SR / 2].y)
 
     // Row masks of this thread's column segment (bit i = row r0 + i of the region),
     // computed once so that the unrolled row loops below test one bit per row:
@@ -194,7 +229,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
             s = __fadd_rn(s, S[no + rd * RW + tx]);
             s = __fsub_rn(s, S[no + ru * RW + tx]);
-            k[i] = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
+            KREF(i) = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
             c[i] = (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
         }
         __syncthreads();
@@ -207,14 +242,14 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
             if ((m_int >> i) & 1u) x = __fadd_rn(x, __fmul_rn(dt, __ldcg(F.x2 + o)));
             c[i] = x;
-            k[i] = x;
+            KREF(i) = x;
         }
     } else {
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
             c[i] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            k[i] = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
+            KREF(i) = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
         }
     }
 #pragma unroll
@@ -224,10 +259,10 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // ------------------------------------------------------------------ sweeps
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
     if (edge_cta) {
-        run_sweeps<DIFF, true, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, m_int, gy0, gc, rows, cols, F.s_lr,
+        run_sweeps<DIFF, true, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, m_int, gy0, gc, rows, cols, F.s_lr,
                                        F.s_tb, F.a, F.dh, F.dl, F.rf);
     } else {
-        run_sweeps<DIFF, false, SR, RH>(k, co, no, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
+        run_sweeps<DIFF, false, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
                                         F.s_tb, F.a, F.dh, F.dl, F.rf);
     }
     // final values of this thread's column (S + co is complete after the last barrier)
@@ -248,7 +283,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         if (ko) {
 #pragma unroll
             for (int i = 0; i < SR; ++i)
-                if ((m_out >> i) & 1u) ko[o0 + (size_t)i * pitch] = k[i];
+                if ((m_out >> i) & 1u) ko[o0 + (size_t)i * pitch] = KREF(i);
         }
     }
     if (F.epilogue && col_out) {
@@ -309,16 +344,18 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             const int r = r0 + i, gr = gy0 + r;
             if (r < H || r >= H + F.tile_h || !col_int || gr < 1 || gr > rows - 2) continue;
             const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
-            float sres = k[i] + S[co + r * RW + txr];
+            float sres = KREF(i) + S[co + r * RW + txr];
             sres += S[co + r * RW + txl];
             sres += S[co + rd * RW + tx];
             sres += S[co + ru * RW + tx];
             const float res = sres - 4.f * c[i];
             rnum = fmaf(res, res, rnum);
-            rden = fmaf(k[i], k[i], rden);
+            rden = fmaf(KREF(i), KREF(i), rden);
         }
     }
 }
+
+#undef KREF
 
 // One launch = one pass over the tiles of up to kMaxStencilFields fields.
 template <int TY, int SR, bool DIFF>
