@@ -68,6 +68,14 @@ class fs_device_view(C.Structure):
                 ("pitch", C.c_int), ("stream", C.c_void_p)]
 
 
+FS_SOURCE_DENSITY, FS_SOURCE_VELOCITY = 0, 1
+
+
+class fs_source_event(C.Structure):
+    _fields_ = [("step", C.c_int), ("kind", C.c_int), ("i", C.c_int), ("j", C.c_int), ("value", C.c_float),
+                ("value2", C.c_float)]
+
+
 # Every symbol the C header declares, with its ctypes signature.
 _P = C.c_void_p
 _F = C.c_float
@@ -86,6 +94,10 @@ SIGNATURES = {
     "fs_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
     "fs_device_view_get": (C.c_int, [_P, C.POINTER(fs_device_view)]),
     "fs_stage": (C.c_int, [_P, _I, _F, _F]),
+    "fs_add_density_source": (C.c_int, [_P, _I, _I, _F]),
+    "fs_add_velocity_source": (C.c_int, [_P, _I, _I, _F, _F]),
+    "fs_update": (C.c_int, [_P, _F, _F, _F]),
+    "fs_run_script": (C.c_int, [_P, C.POINTER(fs_source_event), _I, _I, _F, _F, _F]),
     "fs_profile_step": (C.c_int, [_P, _F, _F, _F, C.POINTER(fs_kernel_times)]),
     "fs_project_noalloc": (C.c_int, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
     "fs_batch_create": (C.c_int, [C.POINTER(fs_config), _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P)]),
@@ -225,6 +237,25 @@ class Solver:
 
     def step(self, diffusion_rate, viscosity, dt, nsteps=1, sync=True):
         _check(self._lib.fs_step(self._h, diffusion_rate, viscosity, dt, nsteps))
+        if sync:
+            _check(self._lib.fs_sync(self._h))
+
+    # ---- the reference's simulation driver (src/simulation.cpp:44-64), device-resident
+    def add_density_source(self, i, j, value):
+        _check(self._lib.fs_add_density_source(self._h, int(i), int(j), float(value)))
+
+    def add_velocity_source(self, i, j, horizontal, vertical):
+        _check(self._lib.fs_add_velocity_source(self._h, int(i), int(j), float(horizontal), float(vertical)))
+
+    def update(self, diffusion_rate, viscosity, dt, sync=True):
+        _check(self._lib.fs_update(self._h, diffusion_rate, viscosity, dt))
+        if sync:
+            _check(self._lib.fs_sync(self._h))
+
+    def run_script(self, events, nsteps, diffusion_rate, viscosity, dt, sync=True):
+        """events: sequence of (step, kind, i, j, value, value2), sorted by step."""
+        arr = (fs_source_event * max(1, len(events)))(*[fs_source_event(*e) for e in events])
+        _check(self._lib.fs_run_script(self._h, arr, len(events), nsteps, diffusion_rate, viscosity, dt))
         if sync:
             _check(self._lib.fs_sync(self._h))
 

@@ -121,6 +121,8 @@ struct fs_solver {
     } net;
     float* pguess = nullptr;  // fine starting pressure built from the network
     SolveCtrl* host_ctrl = nullptr;  // pinned mirror of a control block (learned cycles)
+    fs_source_event* d_events = nullptr;  // device copy of a source script
+    int d_events_cap = 0;
     bool net_ready = false;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -769,6 +771,54 @@ int copy_dd(fs_solver* s, float* dst, const float* src) {
 
 }  // namespace
 
+namespace {
+
+// One source event, simulation.cpp:44-51: source(i, j) += value * width * height with
+// width = cols and height = rows converted to float, multiplied left to right.
+__device__ void apply_source_event(const fs_source_event& ev, float* sd, float* su, float* sv, int rows, int cols,
+                                   int pitch) {
+    if (ev.i < 0 || ev.i >= rows || ev.j < 0 || ev.j >= cols) return;
+    const size_t o = (size_t)ev.i * pitch + ev.j;
+    const float w = (float)cols, h = (float)rows;
+    if (ev.kind == FS_SOURCE_DENSITY) {
+        sd[o] = __fadd_rn(sd[o], __fmul_rn(__fmul_rn(ev.value, w), h));
+    } else {
+        su[o] = __fadd_rn(su[o], __fmul_rn(__fmul_rn(ev.value, w), h));
+        sv[o] = __fadd_rn(sv[o], __fmul_rn(__fmul_rn(ev.value2, w), h));
+    }
+}
+
+// Events are applied by one thread in array order: the additions to a cell happen in
+// the order the reference's calls would make them.
+__global__ void source_events_kernel(const fs_source_event* __restrict__ ev, int begin, int end, float* sd, float* su,
+                                     float* sv, int rows, int cols, int pitch) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int k = begin; k < end; ++k) apply_source_event(ev[k], sd, su, sv, rows, cols, pitch);
+}
+
+__global__ void source_event_kernel(fs_source_event ev, float* sd, float* su, float* sv, int rows, int cols,
+                                    int pitch) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) apply_source_event(ev, sd, su, sv, rows, cols, pitch);
+}
+
+int add_source(fs_solver* s, const fs_source_event& ev) {
+    if (ev.i < 0 || ev.i >= s->rows || ev.j < 0 || ev.j >= s->cols)
+        return fail(FS_ERR_ARG, "source cell outside the grid");
+    DeviceGuard g(s->device);
+    source_event_kernel<<<1, 32, 0, s->stream>>>(ev, s->src[F_D], s->src[F_U], s->src[F_V], s->rows, s->cols,
+                                                 s->pitch);
+    CK(cudaGetLastError());
+    s->stats.kernel_launches++;
+    return FS_OK;
+}
+
+int clear_sources(fs_solver* s) {
+    for (int f = 0; f < 3; ++f) CK(cudaMemsetAsync(s->src[f], 0, s->field_floats * sizeof(float), s->stream));
+    return FS_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* fs_version(void) { return "fluid2d_gb300 " FS_VERSION " sm_103a"; }
@@ -957,6 +1007,7 @@ int fs_destroy(fs_solver* s) {
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->net.mem) cudaFree(s->net.mem);
     if (s->host_ctrl) cudaFreeHost(s->host_ctrl);
+    if (s->d_events) cudaFree(s->d_events);
     cudaFree(s->slab);
     delete s;
     return FS_OK;
@@ -1020,6 +1071,69 @@ int fs_solve_host(fs_solver* s, float* density, const float* density_source, flo
         return rc;
     CK(cudaStreamSynchronize(s->stream));
     return check_flags(s);
+}
+
+int fs_add_density_source(fs_solver* s, int i, int j, float value) {
+    if (!s) return fail(FS_ERR_ARG, "fs_add_density_source: null handle");
+    fs_source_event ev{0, FS_SOURCE_DENSITY, i, j, value, 0.f};
+    return add_source(s, ev);
+}
+
+int fs_add_velocity_source(fs_solver* s, int i, int j, float horizontal, float vertical) {
+    if (!s) return fail(FS_ERR_ARG, "fs_add_velocity_source: null handle");
+    fs_source_event ev{0, FS_SOURCE_VELOCITY, i, j, horizontal, vertical};
+    return add_source(s, ev);
+}
+
+int fs_update(fs_solver* s, float diffusion_rate, float viscosity, float dt) {
+    if (!s) return fail(FS_ERR_ARG, "fs_update: null handle");
+    DeviceGuard g(s->device);
+    int rc = run_steps(s, diffusion_rate, viscosity, dt, 1);
+    return rc != FS_OK ? rc : clear_sources(s);
+}
+
+int fs_run_script(fs_solver* s, const fs_source_event* events, int count, int nsteps, float diffusion_rate,
+                  float viscosity, float dt) {
+    if (!s || count < 0 || nsteps < 0 || (count > 0 && !events)) return fail(FS_ERR_ARG, "fs_run_script: bad argument");
+    for (int k = 0; k < count; ++k) {
+        const fs_source_event& e = events[k];
+        if (e.step < 0 || e.step >= nsteps || (k > 0 && e.step < events[k - 1].step))
+            return fail(FS_ERR_ARG, "fs_run_script: events must be sorted by step, within [0, nsteps)");
+        if ((e.kind != FS_SOURCE_DENSITY && e.kind != FS_SOURCE_VELOCITY) || e.i < 0 || e.i >= s->rows || e.j < 0 ||
+            e.j >= s->cols)
+            return fail(FS_ERR_ARG, "fs_run_script: bad event kind or cell");
+    }
+    DeviceGuard g(s->device);
+    if (count > s->d_events_cap) {
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->d_events) cudaFree(s->d_events);
+        s->d_events = nullptr;
+        s->d_events_cap = 0;
+        cudaError_t e = cudaMalloc(&s->d_events, (size_t)count * sizeof(fs_source_event));
+        if (e != cudaSuccess) return cuda_fail(e, "fs_run_script: cudaMalloc");
+        s->d_events_cap = count;
+    }
+    if (count > 0) {
+        // the stream may still read an earlier script: wait before overwriting it
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaMemcpy(s->d_events, events, (size_t)count * sizeof(fs_source_event), cudaMemcpyHostToDevice));
+    }
+    int begin = 0;
+    for (int k = 0; k < nsteps; ++k) {
+        int end = begin;
+        while (end < count && events[end].step == k) ++end;
+        if (end > begin) {
+            source_events_kernel<<<1, 32, 0, s->stream>>>(s->d_events, begin, end, s->src[F_D], s->src[F_U],
+                                                          s->src[F_V], s->rows, s->cols, s->pitch);
+            CK(cudaGetLastError());
+            s->stats.kernel_launches++;
+        }
+        begin = end;
+        int rc = run_steps(s, diffusion_rate, viscosity, dt, 1);
+        if (rc != FS_OK) return rc;
+        if ((rc = clear_sources(s)) != FS_OK) return rc;
+    }
+    return FS_OK;
 }
 
 int fs_stage(fs_solver* s, int stage, float rate, float dt) {

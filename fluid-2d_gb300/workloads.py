@@ -180,3 +180,23 @@ def random_state(rows, cols, seed, vmax=1.0):
     rng = np.random.default_rng(seed)
     f = lambda lo, hi: rng.uniform(lo, hi, size=(rows, cols)).astype(np.float32)
     return f(0, 1), f(-vmax, vmax), f(-vmax, vmax), f(0, 10), f(-1, 1), f(-1, 1)
+
+
+def drag_script(rows, cols, nsteps, seed=0, density=0.075, speed=0.05):
+    """A seeded stand-in for the reference app's mouse drag (src/app.cpp:100-118): a
+    manipulation point moves along a smooth random path; every step it adds `density`
+    at its cell and `speed` times its unit movement direction as velocity. Returns
+    events (step, kind, i, j, value, value2) sorted by step."""
+    rng = np.random.default_rng(seed)
+    y, x = rng.uniform(0.3, 0.7) * rows, rng.uniform(0.3, 0.7) * cols
+    ang = rng.uniform(0, 2 * np.pi)
+    events = []
+    for k in range(nsteps):
+        ang += rng.normal(0.0, 0.3)
+        dy, dx = np.sin(ang), np.cos(ang)
+        y = min(max(y + 0.8 * dy, 1.0), rows - 2.0)
+        x = min(max(x + 0.8 * dx, 1.0), cols - 2.0)
+        i, j = int(y), int(x)
+        events.append((k, 0, i, j, float(density), 0.0))
+        events.append((k, 1, i, j, float(speed * dx), float(speed * dy)))
+    return events

@@ -130,6 +130,34 @@ FS_API int fs_create(const fs_config* cfg, fs_solver** out);
  * Writes 0 when no device is usable. */
 FS_API int fs_gauss_seidel_max_size(int* n);
 
+/* Device-resident simulation driver: the reference's simulation::add_*_source and
+ * simulation::update (src/simulation.cpp:44-64) on the handle's source grids, so a frame
+ * loop never moves a field through host memory. A source event adds value * cols * rows
+ * (float arithmetic, in that order, as simulation.cpp:45,49-50) to cell (i, j) of the
+ * density source, or the horizontal / vertical velocity sources. */
+#define FS_SOURCE_DENSITY 0
+#define FS_SOURCE_VELOCITY 1
+typedef struct fs_source_event {
+    int step;     /* fs_run_script: the step (0-based within the call) it belongs to */
+    int kind;     /* FS_SOURCE_DENSITY or FS_SOURCE_VELOCITY */
+    int i, j;     /* cell (row, column), boundary included */
+    float value;  /* density, or horizontal velocity */
+    float value2; /* vertical velocity (FS_SOURCE_VELOCITY) */
+} fs_source_event;
+
+/* simulation::add_density_source / add_velocity_source (simulation.cpp:44-51), on the
+ * device, asynchronous on the handle's stream. */
+FS_API int fs_add_density_source(fs_solver* s, int i, int j, float value);
+FS_API int fs_add_velocity_source(fs_solver* s, int i, int j, float horizontal, float vertical);
+/* simulation::update (simulation.cpp:53-64): one step with the accumulated sources, then
+ * the three source grids cleared. Asynchronous. */
+FS_API int fs_update(fs_solver* s, float diffusion_rate, float viscosity, float dt);
+/* nsteps updates driven by a script: before step k the events with step == k are added
+ * in array order (events must be sorted by step; steps outside [0, nsteps) are an
+ * error), then the step runs and the sources are cleared. Asynchronous. */
+FS_API int fs_run_script(fs_solver* s, const fs_source_event* events, int count, int nsteps,
+                         float diffusion_rate, float viscosity, float dt);
+
 /* Replaces fluid_solver_gpu::~fluid_solver_gpu (fluid_solver_gpu.cu:220). NULL is a no-op. */
 FS_API int fs_destroy(fs_solver* s);
 

@@ -227,3 +227,29 @@ def render_velocity_lines(u, v, hscale, vscale):
     for c in "rgba":
         out[c] = 255
     return out
+
+
+def simulation_run(d, u, v, events, nsteps, diff, visc, dt, kd=15, kp=20, smooth=True):
+    """The reference's simulation driver around the GPU-semantics step: before step k
+    the events of step k are added to zeroed source grids in order, source(i, j) +=
+    value * width * height in float32 (src/simulation.cpp:44-51), then the step runs and
+    the sources are cleared (src/simulation.cpp:53-64). events: (step, kind, i, j,
+    value, value2), kind 0 = density, 1 = velocity."""
+    rows, cols = d.shape
+    w, h = np.float32(cols), np.float32(rows)
+    d, u, v = (_c(a) for a in (d, u, v))
+    k = 0
+    for step in range(nsteps):
+        ds = np.zeros_like(d)
+        us = np.zeros_like(d)
+        vs = np.zeros_like(d)
+        while k < len(events) and events[k][0] == step:
+            _, kind, i, j, a, b = events[k]
+            if kind == 0:
+                ds[i, j] = np.float32(ds[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
+            else:
+                us[i, j] = np.float32(us[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
+                vs[i, j] = np.float32(vs[i, j] + np.float32(np.float32(np.float32(b) * w) * h))
+            k += 1
+        d, u, v = gpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=kd, kp=kp, smooth=smooth)
+    return d, u, v
