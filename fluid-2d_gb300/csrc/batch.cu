@@ -6,9 +6,13 @@
 // the same stage sequence as a single handle, but each sub-step is ONE launch over
 // all grids: the stencil passes walk a device-resident table of per-grid field
 // descriptors (tiles of all grids concatenated, one CTA per tile, a tile -> field
-// map), and the advection stages walk a table of per-grid jobs (a block -> job map). The whole step is captured
-// once as a CUDA graph. Grids share dt, the rates and the sweep counts; each grid has
-// its own size, state and sources.
+// map), and the advection stages walk a table of per-grid jobs (a block -> job map).
+// The grids are dealt to a few lanes (longest-processing-time first, by cells) and each
+// lane runs its own sequence of launches on its own stream, so one lane's small final
+// wave overlaps another lane's work instead of idling the GPU between sub-steps. The
+// whole step, lanes forked from and joined back to the batch's stream, is captured once
+// as a CUDA graph. Grids share dt, the rates and the sweep counts; each grid has its own
+// size, state and sources.
 //
 // Memory: one slab, field-major — for each of the 21 per-grid field kinds, the
 // buffers of all grids follow each other — so e.g. all splat accumulators form one
@@ -63,10 +67,19 @@ struct fs_batch {
         int nfields, total;
         bool diffuse;
     };
-    std::vector<Pass> passes;  // diffusion passes, then project 1, then project 2
+    // one lane: its grids, its passes (diffusion, project 1, project 2) and advection
+    // jobs, and the stream it runs on (lane 0: the batch's stream)
+    struct Lane {
+        std::vector<int> grids;
+        std::vector<Pass> passes;
+        size_t job_off[3] = {}, jprefix_off[3] = {}, jmap_off[3] = {};
+        int job_blocks[3] = {};
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Lane> lanes;
+    cudaEvent_t fork = nullptr;
     int n_diffuse = 0, n_project = 0;
-    size_t job_off[3] = {}, jprefix_off[3] = {}, jmap_off[3] = {};
-    int job_blocks[3] = {};
     void* d_plan = nullptr;
     size_t d_plan_bytes = 0;
     StencilField* d_tab = nullptr;
@@ -84,6 +97,8 @@ namespace {
 
 int fail(int code, const char* msg) { return record_error(code, msg); }
 
+constexpr int kBatchLanes = 4;
+
 // Builds every table of one step for (diff, visc, dt) and uploads them.
 int build_plan(fs_batch* b, float diff, float visc, float dt) {
     b->h_tab.clear();
@@ -91,131 +106,134 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     b->h_jobs.clear();
     b->h_jprefix.clear();
     b->h_map.clear();
-    b->passes.clear();
-    const int n = b->count;
     const int K = b->sweeps;
-    // ---- diffusion passes over all grids x {d, u, v}; add_sources fused in pass 0
     const std::vector<int> dplan = plan_passes(b->cfg.diffuse_iterations, K);
+    const std::vector<int> pplan = plan_passes(b->cfg.pressure_iterations, K);
     b->n_diffuse = (int)dplan.size();
+    b->n_project = (int)pplan.size();
     const int dkinds[3][5] = {{K_ST_D, K_SRC_D, K_X0_D, K_PP_D0, K_PP_D1},
                               {K_ST_U, K_SRC_U, K_X0_U, K_PP_U0, K_PP_U1},
                               {K_ST_V, K_SRC_V, K_X0_V, K_PP_V0, K_PP_V1}};
     const float rates[3] = {diff, visc, visc};
     const int modes[3] = {BND_CONT, BND_OPP_H, BND_OPP_V};
-    for (size_t pass = 0; pass < dplan.size(); ++pass) {
-        fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, true};
-        int tiles = 0;
-        for (int g = 0; g < n; ++g)
-            for (int q = 0; q < 3; ++q) {
-                StencilField f{};
-                field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows, dplan[pass]);
-                field_diffusion(f, b->rows[g], b->cols[g], rates[q], dt);
-                f.s_lr = bnd_sign_lr(modes[q]);
-                f.s_tb = bnd_sign_tb(modes[q]);
-                f.sweeps = dplan[pass];
-                f.dt = dt;
-                const int* k = dkinds[q];
-                f.x = pass == 0 ? b->fld(k[0], g) : b->fld(k[3 + ((pass - 1) & 1)], g);
-                f.y = b->fld(k[3 + (pass & 1)], g);
-                if (pass == 0) {
-                    f.kind = PASS_DIFFUSE_FIRST;
-                    f.x2 = b->fld(k[1], g);
-                    f.cst_out = b->fld(k[2], g);
-                } else {
-                    f.kind = PASS_DIFFUSE;
-                    f.cst = b->fld(k[2], g);
-                }
-                b->h_prefix.push_back(tiles);
-                tiles += f.tiles_x * f.tiles_y;
-                b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
-                b->h_tab.push_back(f);
-                P.nfields++;
-            }
-        b->h_prefix.push_back(tiles);
-        P.total = tiles;
-        b->passes.push_back(P);
-    }
     const int dlast = (b->n_diffuse - 1) & 1;  // ping-pong buffer holding the diffusion result
-    // ---- two projections over all grids (one pressure field each)
-    const std::vector<int> pplan = plan_passes(b->cfg.pressure_iterations, K);
-    b->n_project = (int)pplan.size();
-    for (int proj = 0; proj < 2; ++proj) {
-        for (int pass = 0; pass < b->n_project; ++pass) {
-            const bool last = pass == b->n_project - 1;
-            fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, false};
+    for (fs_batch::Lane& L : b->lanes) {
+        L.passes.clear();
+        // ---- diffusion passes over the lane's grids x {d, u, v}; add_sources fused in pass 0
+        for (size_t pass = 0; pass < dplan.size(); ++pass) {
+            fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, true};
             int tiles = 0;
-            for (int g = 0; g < n; ++g) {
-                StencilField f{};
-                field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows, pplan[pass] + (last ? 1 : 0));
-                const float h = grid_spacing(b->rows[g], b->cols[g]);
-                f.s_lr = f.s_tb = 1.f;
-                f.sweeps = pplan[pass];
-                f.cdiv = -0.5f * h;
-                f.h = h;
-                const float* uin = proj == 0 ? b->fld(K_PP_U0 + dlast, g) : b->fld(K_VEL_U, g);
-                const float* vin = proj == 0 ? b->fld(K_PP_V0 + dlast, g) : b->fld(K_VEL_V, g);
-                if (pass == 0) {
-                    f.kind = PASS_PRESSURE_FIRST;
-                    f.x = uin;
-                    f.x2 = vin;
-                    f.cst_out = b->fld(K_DIV, g);
-                } else {
-                    f.kind = PASS_PRESSURE;
-                    f.x = b->fld(K_P0 + ((pass - 1) & 1), g);
-                    f.cst = b->fld(K_DIV, g);
+            for (int g : L.grids)
+                for (int q = 0; q < 3; ++q) {
+                    StencilField f{};
+                    field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows, dplan[pass]);
+                    field_diffusion(f, b->rows[g], b->cols[g], rates[q], dt);
+                    f.s_lr = bnd_sign_lr(modes[q]);
+                    f.s_tb = bnd_sign_tb(modes[q]);
+                    f.sweeps = dplan[pass];
+                    f.dt = dt;
+                    const int* k = dkinds[q];
+                    f.x = pass == 0 ? b->fld(k[0], g) : b->fld(k[3 + ((pass - 1) & 1)], g);
+                    f.y = b->fld(k[3 + (pass & 1)], g);
+                    if (pass == 0) {
+                        f.kind = PASS_DIFFUSE_FIRST;
+                        f.x2 = b->fld(k[1], g);
+                        f.cst_out = b->fld(k[2], g);
+                    } else {
+                        f.kind = PASS_DIFFUSE;
+                        f.cst = b->fld(k[2], g);
+                    }
+                    b->h_prefix.push_back(tiles);
+                    tiles += f.tiles_x * f.tiles_y;
+                    b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
+                    b->h_tab.push_back(f);
+                    P.nfields++;
                 }
-                f.y = last ? nullptr : b->fld(K_P0 + (pass & 1), g);
-                if (last) {
-                    f.epilogue = 1;
-                    f.u_in = uin;
-                    f.v_in = vin;
-                    f.u_out = b->fld(K_ST_U, g);
-                    f.v_out = b->fld(K_ST_V, g);
-                    f.nonfinite = b->cfg.check_finite ? b->flags : nullptr;
-                }
-                b->h_prefix.push_back(tiles);
-                tiles += f.tiles_x * f.tiles_y;
-                b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
-                b->h_tab.push_back(f);
-                P.nfields++;
-            }
             b->h_prefix.push_back(tiles);
             P.total = tiles;
-            b->passes.push_back(P);
+            L.passes.push_back(P);
         }
-    }
-    // ---- advection jobs: splat, finish, velocity backtrace
-    for (int op = 0; op < 3; ++op) {
-        b->job_off[op] = b->h_jobs.size();
-        b->jprefix_off[op] = b->h_jprefix.size();
-        b->jmap_off[op] = b->h_map.size();
-        int blocks = 0;
-        for (int g = 0; g < n; ++g) {
-            AdvectJob J{};
-            J.A = make_advect_args(b->rows[g], b->cols[g], b->pitch[g], dt);
-            J.smooth = b->cfg.smooth;
-            if (op == 0) {
-                J.in0 = b->fld(K_PP_D0 + dlast, g);
-                J.in1 = b->fld(K_ST_U, g);
-                J.in2 = b->fld(K_ST_V, g);
-                J.out0 = b->fld(K_ACC, g);
-            } else if (op == 1) {
-                J.in0 = b->fld(K_ACC, g);
-                J.out0 = b->fld(K_ST_D, g);
-            } else {
-                J.in0 = b->fld(K_ST_U, g);
-                J.in1 = b->fld(K_ST_V, g);
-                J.out0 = b->fld(K_VEL_U, g);
-                J.out1 = b->fld(K_VEL_V, g);
+        // ---- two projections over the lane's grids (one pressure field each)
+        for (int proj = 0; proj < 2; ++proj) {
+            for (int pass = 0; pass < b->n_project; ++pass) {
+                const bool last = pass == b->n_project - 1;
+                fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, false};
+                int tiles = 0;
+                for (int g : L.grids) {
+                    StencilField f{};
+                    field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows,
+                                   pplan[pass] + (last ? 1 : 0));
+                    const float h = grid_spacing(b->rows[g], b->cols[g]);
+                    f.s_lr = f.s_tb = 1.f;
+                    f.sweeps = pplan[pass];
+                    f.cdiv = -0.5f * h;
+                    f.h = h;
+                    const float* uin = proj == 0 ? b->fld(K_PP_U0 + dlast, g) : b->fld(K_VEL_U, g);
+                    const float* vin = proj == 0 ? b->fld(K_PP_V0 + dlast, g) : b->fld(K_VEL_V, g);
+                    if (pass == 0) {
+                        f.kind = PASS_PRESSURE_FIRST;
+                        f.x = uin;
+                        f.x2 = vin;
+                        f.cst_out = b->fld(K_DIV, g);
+                    } else {
+                        f.kind = PASS_PRESSURE;
+                        f.x = b->fld(K_P0 + ((pass - 1) & 1), g);
+                        f.cst = b->fld(K_DIV, g);
+                    }
+                    f.y = last ? nullptr : b->fld(K_P0 + (pass & 1), g);
+                    if (last) {
+                        f.epilogue = 1;
+                        f.u_in = uin;
+                        f.v_in = vin;
+                        f.u_out = b->fld(K_ST_U, g);
+                        f.v_out = b->fld(K_ST_V, g);
+                        f.nonfinite = b->cfg.check_finite ? b->flags : nullptr;
+                    }
+                    b->h_prefix.push_back(tiles);
+                    tiles += f.tiles_x * f.tiles_y;
+                    b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
+                    b->h_tab.push_back(f);
+                    P.nfields++;
+                }
+                b->h_prefix.push_back(tiles);
+                P.total = tiles;
+                L.passes.push_back(P);
+            }
+        }
+        // ---- advection jobs: splat, finish, velocity backtrace
+        for (int op = 0; op < 3; ++op) {
+            L.job_off[op] = b->h_jobs.size();
+            L.jprefix_off[op] = b->h_jprefix.size();
+            L.jmap_off[op] = b->h_map.size();
+            int blocks = 0;
+            int jobs = 0;
+            for (int g : L.grids) {
+                AdvectJob J{};
+                J.A = make_advect_args(b->rows[g], b->cols[g], b->pitch[g], dt);
+                J.smooth = b->cfg.smooth;
+                if (op == 0) {
+                    J.in0 = b->fld(K_PP_D0 + dlast, g);
+                    J.in1 = b->fld(K_ST_U, g);
+                    J.in2 = b->fld(K_ST_V, g);
+                    J.out0 = b->fld(K_ACC, g);
+                } else if (op == 1) {
+                    J.in0 = b->fld(K_ACC, g);
+                    J.out0 = b->fld(K_ST_D, g);
+                } else {
+                    J.in0 = b->fld(K_ST_U, g);
+                    J.in1 = b->fld(K_ST_V, g);
+                    J.out0 = b->fld(K_VEL_U, g);
+                    J.out1 = b->fld(K_VEL_V, g);
+                }
+                b->h_jprefix.push_back(blocks);
+                const int nb = advect_batch_blocks(b->rows[g], b->cols[g]);
+                blocks += nb;
+                b->h_map.insert(b->h_map.end(), nb, jobs++);
+                b->h_jobs.push_back(J);
             }
             b->h_jprefix.push_back(blocks);
-            const int nb = advect_batch_blocks(b->rows[g], b->cols[g]);
-            blocks += nb;
-            b->h_map.insert(b->h_map.end(), nb, g);
-            b->h_jobs.push_back(J);
+            L.job_blocks[op] = blocks;
         }
-        b->h_jprefix.push_back(blocks);
-        b->job_blocks[op] = blocks;
     }
     // ---- upload (one buffer, tables first)
     const size_t tab_bytes = b->h_tab.size() * sizeof(StencilField);
@@ -247,32 +265,49 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     return FS_OK;
 }
 
-int enqueue_pass(fs_batch* b, const fs_batch::Pass& P, int& launches) {
+int enqueue_pass(fs_batch* b, const fs_batch::Pass& P, cudaStream_t st, int& launches) {
     FS_CK(launch_stencil_table(b->d_tab + P.tab, b->d_prefix + P.prefix, b->d_map + P.map, P.total, P.diffuse,
-                               b->tile_rows, b->stream));
+                               b->tile_rows, st));
     launches++;
     return FS_OK;
 }
 
-int enqueue_step(fs_batch* b, int& launches) {
+int enqueue_lane(fs_batch* b, const fs_batch::Lane& L, int& launches) {
     int rc;
+    const cudaStream_t st = L.stream;
     size_t pi = 0;
     for (int k = 0; k < b->n_diffuse; ++k)
-        if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;
-    FS_CK(cudaMemsetAsync(b->slab + (size_t)K_ACC * b->range_floats, 0, b->range_floats * sizeof(float), b->stream));
+        if ((rc = enqueue_pass(b, L.passes[pi++], st, launches)) != FS_OK) return rc;
     int* nf = b->cfg.check_finite ? b->flags : nullptr;
-    FS_CK(launch_advect_batch(0, b->d_jobs + b->job_off[0], b->d_jprefix + b->jprefix_off[0],
-                              b->d_map + b->jmap_off[0], b->job_blocks[0], nullptr, b->stream));
-    FS_CK(launch_advect_batch(1, b->d_jobs + b->job_off[1], b->d_jprefix + b->jprefix_off[1],
-                              b->d_map + b->jmap_off[1], b->job_blocks[1], nf, b->stream));
+    FS_CK(launch_advect_batch(0, b->d_jobs + L.job_off[0], b->d_jprefix + L.jprefix_off[0],
+                              b->d_map + L.jmap_off[0], L.job_blocks[0], nullptr, st));
+    FS_CK(launch_advect_batch(1, b->d_jobs + L.job_off[1], b->d_jprefix + L.jprefix_off[1],
+                              b->d_map + L.jmap_off[1], L.job_blocks[1], nf, st));
     launches += 2;
     for (int k = 0; k < b->n_project; ++k)
-        if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;
-    FS_CK(launch_advect_batch(2, b->d_jobs + b->job_off[2], b->d_jprefix + b->jprefix_off[2],
-                              b->d_map + b->jmap_off[2], b->job_blocks[2], nullptr, b->stream));
+        if ((rc = enqueue_pass(b, L.passes[pi++], st, launches)) != FS_OK) return rc;
+    FS_CK(launch_advect_batch(2, b->d_jobs + L.job_off[2], b->d_jprefix + L.jprefix_off[2],
+                              b->d_map + L.jmap_off[2], L.job_blocks[2], nullptr, st));
     launches++;
     for (int k = 0; k < b->n_project; ++k)
-        if ((rc = enqueue_pass(b, b->passes[pi++], launches)) != FS_OK) return rc;
+        if ((rc = enqueue_pass(b, L.passes[pi++], st, launches)) != FS_OK) return rc;
+    return FS_OK;
+}
+
+// One step: clear every splat accumulator, fork the lanes from the batch's stream, run
+// each lane's sequence on its stream, join them back.
+int enqueue_step(fs_batch* b, int& launches) {
+    int rc;
+    FS_CK(cudaMemsetAsync(b->slab + (size_t)K_ACC * b->range_floats, 0, b->range_floats * sizeof(float), b->stream));
+    const size_t nl = b->lanes.size();
+    if (nl > 1) FS_CK(cudaEventRecord(b->fork, b->stream));
+    for (size_t l = 1; l < nl; ++l) FS_CK(cudaStreamWaitEvent(b->lanes[l].stream, b->fork, 0));
+    for (size_t l = 0; l < nl; ++l)
+        if ((rc = enqueue_lane(b, b->lanes[l], launches)) != FS_OK) return rc;
+    for (size_t l = 1; l < nl; ++l) {
+        FS_CK(cudaEventRecord(b->lanes[l].done, b->lanes[l].stream));
+        FS_CK(cudaStreamWaitEvent(b->stream, b->lanes[l].done, 0));
+    }
     return FS_OK;
 }
 
@@ -351,6 +386,34 @@ int fs_batch_create(const fs_config* cfg, int count, const int* rows, const int*
         return rc;
     }
     b->flags = reinterpret_cast<int*>(b->slab + (size_t)K_COUNT * total);
+    // lanes: grids dealt longest-first to the lane with the fewest cells so far
+    const int nlanes = std::min(kBatchLanes, count);
+    b->lanes.resize(nlanes);
+    std::vector<int> order(count);
+    for (int g = 0; g < count; ++g) order[g] = g;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return (long long)rows[x] * cols[x] > (long long)rows[y] * cols[y];
+    });
+    std::vector<long long> load(nlanes, 0);
+    for (int g : order) {
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        b->lanes[l].grids.push_back(g);
+        load[l] += (long long)rows[g] * cols[g];
+    }
+    for (auto& L : b->lanes) std::sort(L.grids.begin(), L.grids.end());
+    b->lanes[0].stream = b->stream;
+    int rc = FS_OK;
+    for (int l = 1; l < nlanes && rc == FS_OK; ++l) {
+        if ((e = cudaStreamCreateWithFlags(&b->lanes[l].stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&b->lanes[l].done, cudaEventDisableTiming)) != cudaSuccess)
+            rc = cuda_error(e, "fs_batch_create: lane streams");
+    }
+    if (rc == FS_OK && nlanes > 1 && (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess)
+        rc = cuda_error(e, "fs_batch_create: lane events");
+    if (rc != FS_OK) {
+        fs_batch_destroy(b);
+        return rc;
+    }
     *out = b;
     return FS_OK;
 }
@@ -361,6 +424,11 @@ int fs_batch_destroy(fs_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graph(b);
     if (b->d_plan) cudaFree(b->d_plan);
+    for (size_t l = 1; l < b->lanes.size(); ++l) {
+        if (b->lanes[l].stream) cudaStreamDestroy(b->lanes[l].stream);
+        if (b->lanes[l].done) cudaEventDestroy(b->lanes[l].done);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->stream) cudaStreamDestroy(b->stream);
     cudaFree(b->slab);
     delete b;
@@ -421,7 +489,8 @@ int fs_batch_step(fs_batch* b, float diffusion_rate, float viscosity, float dt, 
             b->graph = g;
             FS_CK(cudaGraphInstantiate(&b->gexec, g, 0));
         } else {
-            launches = b->n_diffuse + 2 * b->n_project + 3;  // stencil passes + three advection launches
+            // stencil passes + three advection launches, per lane
+            launches = (int)b->lanes.size() * (b->n_diffuse + 2 * b->n_project + 3);
         }
         b->launches_per_step = launches;
         b->graph_valid = true;
