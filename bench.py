@@ -223,7 +223,10 @@ def run_reference(a):
     line = {"metric": metric_name(), "value": val, "unit": "cell-steps/s", "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
-            "config": workload_config(a, {"sample_interior": sample.rows - 2}),
+            "config": workload_config(a, {"sample_interior": sample.rows - 2,
+                                          "l2": "not applicable (host cores)",
+                                          "method": "Gauss-Seidel (the reference's host solver), "
+                                                    f"Kd={a.kd} Kp={a.kp}"}),
             "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": 1, "kind": "port",
                              "sample": f"{a.steps} steps of a {sample.rows - 2}^2 grid (same workload family), "
                                        "fluid_solver_cpu.cpp restated (Gauss-Seidel), single thread"},
