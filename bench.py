@@ -677,18 +677,24 @@ def run_learned(a):
         params = np.load(a.load_weights).astype(np.float32)
     else:
         t0 = time.perf_counter()
-        X, T, ginfo = train_warmstart.generate(a.samples, size=a.train_size, steps_per_run=100, seed=100)
+        # the 32^2 coarse grid: 512^2 runs (vortex cores 1-4 % of the side) and, for the
+        # evaluation's sizes, 1024^2 runs with its vortex field (cores 20-80 cells)
+        half = a.samples // 2
+        X1, T1, g1 = train_warmstart.generate(half, size=a.train_size, steps_per_run=100, seed=100, g=32)
+        X2, T2, g2 = train_warmstart.generate(a.samples - half, size=2 * a.train_size, steps_per_run=50, seed=500,
+                                              g=32, rmin=20.0, rmax=80.0, vortices=64)
         t1 = time.perf_counter()
-        params, hist = train_warmstart.train(X, T, epochs=a.epochs, batch=128, lr=1e-3, seed=0)
+        params, hist = train_warmstart.train_sets([(X1, T1), (X2, T2)], epochs=a.epochs, batch=128, lr=1e-3, seed=0)
         t2 = time.perf_counter()
-        base = train_warmstart.evaluate_loss(learned.init_params(0), X[:2048], T[:2048])
-        fin = train_warmstart.evaluate_loss(params, X[:2048], T[:2048])
-        info = {"samples": int(X.shape[0]), "train_size": a.train_size, "gen_s": t1 - t0, "train_s": t2 - t1,
-                "epochs": a.epochs, "generation_sweeps": ginfo["sweeps"],
-                "loss_init": base, "loss_trained": fin, "loss_first_batch": hist[0], "loss_last_batch": hist[-1]}
+        base = [train_warmstart.evaluate_loss(learned.init_params(0), X[:2048], T[:2048]) for X, T in ((X1, T1), (X2, T2))]
+        fin = [train_warmstart.evaluate_loss(params, X[:2048], T[:2048]) for X, T in ((X1, T1), (X2, T2))]
+        info = {"samples": [int(X1.shape[0]), int(X2.shape[0])], "train_sizes": [a.train_size, 2 * a.train_size],
+                "coarse_grids": [32, 32], "gen_s": t1 - t0, "train_s": t2 - t1, "epochs": a.epochs,
+                "generation_sweeps": g1["sweeps"], "loss_init": base, "loss_trained": fin,
+                "loss_first_batch": hist[0], "loss_last_batch": hist[-1]}
         if a.weights:
             np.save(a.weights, params)
-        del X, T
+        del X1, T1, X2, T2
         torch.cuda.empty_cache()
     results = []
     for size in [int(x) for x in a.eval_sizes.split(",")]:

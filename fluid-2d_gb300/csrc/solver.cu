@@ -105,7 +105,7 @@ struct fs_solver {
     // training-data capture: each projection's divergence and starting pressure
     float* cap_div[2] = {};
     float* cap_start[2] = {};
-    // learned warm start (FS_WARM_LEARNED): network state on the FS_NET_GRID^2 grid
+    // learned warm start (FS_WARM_LEARNED): network state on a G x G coarse grid
     struct Net {
         float* params = nullptr;          // FP32 [8][32*9*32 + 32]
         __nv_bfloat16* wpk = nullptr;     // packed BF16 weights, 8 x 9216
@@ -117,6 +117,7 @@ struct fs_solver {
         double* res = nullptr;            // [coarse residual norm^2, energy gain: network, coarse only]
         float* bs = nullptr;              // coarse residual block sums of the current pressure, G*G
         float* yc = nullptr;              // coarse-only correction, G*G*32 (channel 0 used)
+        int G = FS_NET_GRID;              // coarse grid side (32 or 64)
         void* mem = nullptr;
     } net;
     float* pguess = nullptr;  // fine starting pressure built from the network
@@ -277,20 +278,21 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
     return FS_OK;
 }
 
-constexpr int kNetG = FS_NET_GRID;
+constexpr int kNetGMax = FS_NET_GRID_MAX;
 constexpr int kNetC = 32;
 constexpr int kNetLayer = 32 * 9 * 32 + 32;
-constexpr float kNetKappa = kNetG * kNetG / 16.0f;
+// output units of the network on a G x G grid (restriction and prolongation use the same)
+inline float net_kappa(int G) { return (float)G * (float)G / 16.0f; }
 // activation buffers (BF16, 32 channels): xin, e1, pool1, e2, e3, pool2, b1, b2, d1, d2, out
 constexpr int kNetActs = 11;
-inline size_t net_act_pixels(int k) {
+inline size_t net_act_pixels(int k, int G) {
     const int lv[kNetActs] = {0, 0, 1, 1, 1, 2, 2, 2, 1, 0, 0};
-    const int g = kNetG >> lv[k];
+    const int g = G >> lv[k];
     return (size_t)g * g;
 }
 __nv_bfloat16* net_act(fs_solver* s, int k) {
     size_t off = 0;
-    for (int i = 0; i < k; ++i) off += net_act_pixels(i) * kNetC;
+    for (int i = 0; i < k; ++i) off += net_act_pixels(i, s->net.G) * kNetC;
     return s->net.act + off;
 }
 
@@ -324,12 +326,14 @@ constexpr int kCoarseSweeps = 20;
 // Jacobi iteration contracts), or p_cur when neither gets closer, and counts whether the
 // network's candidate won. Does nothing to p_cur once *converged (nullable) is set.
 int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged, Counter& cnt) {
-    CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, kNetG, s->net.bs, s->net.res, s->net.scale,
+    const int G = s->net.G;
+    const float kappa = net_kappa(G);
+    CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
                               net_act(s, 0), converged, s->stream));
     cnt.launches += 2;
     int rc;
     auto conv = [&](int li, int in, int out, int lvl, int up, int skip, int relu, float* yf) {
-        const int g = kNetG >> lvl;
+        const int g = G >> lvl;
         return conv3x3_launch(net_act(s, in), s->net.wpk + (size_t)li * 9216, nullptr,
                               s->net.params + (size_t)li * kNetLayer + 9216, skip >= 0 ? net_act(s, skip) : nullptr,
                               out >= 0 ? net_act(s, out) : nullptr, yf, g, g, g, up, relu, 1, s->net.err, converged,
@@ -337,10 +341,10 @@ int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged,
     };
     // e1 (G) -> pool -> e2, e3 (G/2) -> pool -> b1, b2 (G/4) -> d1 (+e3) -> d2 (+e1) -> out
     if ((rc = conv(0, 0, 1, 0, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = fs_net_avgpool2(net_act(s, 1), net_act(s, 2), kNetG / 2, kNetG / 2, s->stream)) != FS_OK) return rc;
+    if ((rc = fs_net_avgpool2(net_act(s, 1), net_act(s, 2), G / 2, G / 2, s->stream)) != FS_OK) return rc;
     if ((rc = conv(1, 2, 3, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
     if ((rc = conv(2, 3, 4, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = fs_net_avgpool2(net_act(s, 4), net_act(s, 5), kNetG / 4, kNetG / 4, s->stream)) != FS_OK) return rc;
+    if ((rc = fs_net_avgpool2(net_act(s, 4), net_act(s, 5), G / 4, G / 4, s->stream)) != FS_OK) return rc;
     if ((rc = conv(3, 5, 6, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
     if ((rc = conv(4, 6, 7, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
     if ((rc = conv(5, 7, 8, 1, 1, 4, 1, nullptr)) != FS_OK) return rc;
@@ -349,13 +353,13 @@ int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged,
     cnt.launches += 10;
     // candidate A: the network's correction, post-smoothed; B: the coarse smoothing alone
     float* pb = s->p[1];  // free between pressure passes
-    CK(launch_coarse_smooth(s->net.y, s->net.y, s->net.bs, s->net.scale, kNetKappa, kNetG, kCoarseSweeps, converged,
+    CK(launch_coarse_smooth(s->net.y, s->net.y, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
                             s->stream));
-    CK(launch_coarse_smooth(nullptr, s->net.yc, s->net.bs, s->net.scale, kNetKappa, kNetG, kCoarseSweeps, converged,
+    CK(launch_coarse_smooth(nullptr, s->net.yc, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
                             s->stream));
-    CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa, converged,
+    CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
                       s->stream));
-    CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, kNetG, s->net.scale, kNetKappa, converged,
+    CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
                       s->stream));
     CK(cudaMemsetAsync(s->net.res + 1, 0, 2 * sizeof(double), s->stream));
     CK(launch_energy_gain(s->div, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
@@ -855,6 +859,10 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         return fail(FS_ERR_ARG, "fs_create: unknown warm_start mode");
     if (cfg->warm_start == FS_WARM_LEARNED && (cfg->rows != cfg->cols || (cfg->rows - 2) % FS_NET_GRID != 0))
         return fail(FS_ERR_ARG, "fs_create: the learned warm start needs a square grid with interior % 32 == 0");
+    if (cfg->learned_grid != 0 && cfg->learned_grid != FS_NET_GRID && cfg->learned_grid != FS_NET_GRID_MAX)
+        return fail(FS_ERR_ARG, "fs_create: learned_grid must be 0, 32 or 64");
+    if (cfg->warm_start == FS_WARM_LEARNED && cfg->learned_grid > 0 && (cfg->rows - 2) % cfg->learned_grid != 0)
+        return fail(FS_ERR_ARG, "fs_create: the interior must be a multiple of learned_grid");
     if (cfg->tile_rows != 0 && cfg->tile_rows != 64 && cfg->tile_rows != 128)
         return fail(FS_ERR_ARG, "fs_create: tile_rows must be 0, 64 or 128");
     if (cfg->pressure_tolerance < 0.f || cfg->pressure_tolerance != cfg->pressure_tolerance)
@@ -953,10 +961,14 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaStreamCreate");
     if (rc == FS_OK && learned) {
+        // coarse grid: learned_grid, else 32 (a finer 64 grid resolves more modes, but the
+        // network and the coarse smoothing both capture the smooth ones less well there)
+        s->net.G = cfg->learned_grid > 0 ? cfg->learned_grid : FS_NET_GRID;
+        const int G = s->net.G;
         size_t acts = 0;
-        for (int k = 0; k < kNetActs; ++k) acts += net_act_pixels(k) * kNetC;
-        const size_t bytes = (size_t)FS_NET_PARAMS * 4 + 8 * 9216 * 2 + acts * 2 + (size_t)kNetG * kNetG * kNetC * 4 +
-                             256 * 4 + 2 * (size_t)kNetG * kNetG * 4 + (size_t)kNetG * kNetG * kNetC * 4;
+        for (int k = 0; k < kNetActs; ++k) acts += net_act_pixels(k, G) * kNetC;
+        const size_t bytes = (size_t)FS_NET_PARAMS * 4 + 8 * 9216 * 2 + acts * 2 + (size_t)G * G * kNetC * 4 +
+                             256 * 4 + 2 * (size_t)G * G * 4 + (size_t)G * G * kNetC * 4;
         if ((e = cudaMalloc(&s->net.mem, bytes)) != cudaSuccess || (e = cudaMemset(s->net.mem, 0, bytes)) != cudaSuccess) {
             rc = cuda_fail(e, "fs_create: network buffers");
         } else {
@@ -968,13 +980,13 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
             s->net.act = reinterpret_cast<__nv_bfloat16*>(q);
             q += acts * 2;
             s->net.y = reinterpret_cast<float*>(q);
-            q += (size_t)kNetG * kNetG * kNetC * 4;
+            q += (size_t)G * G * kNetC * 4;
             s->net.res = reinterpret_cast<double*>(q);                          // 4 doubles
             s->net.counters = reinterpret_cast<unsigned long long*>(q + 32);    // 2
             s->net.scale = reinterpret_cast<float*>(q + 48);
             s->net.err = reinterpret_cast<int*>(q + 52);
             s->net.bs = reinterpret_cast<float*>(q + 256 * 4);
-            s->net.yc = s->net.bs + 2 * (size_t)kNetG * kNetG;
+            s->net.yc = s->net.bs + 2 * (size_t)G * G;
         }
     }
     if (rc == FS_OK && learned && (e = cudaMallocHost(&s->host_ctrl, sizeof(SolveCtrl))) != cudaSuccess)

@@ -106,6 +106,7 @@ class Net:
 
     B: int
     params: object  # torch float32 [NPARAM]
+    g: int = G      # coarse grid side (32 or 64)
 
     def __post_init__(self):
         import torch
@@ -118,7 +119,8 @@ class Net:
         self.wflip = torch.empty((NLAYER, CH * 9 * CH), dtype=f32, device=dev)
         self.wflip_pk = torch.empty((NLAYER, CH * 9 * CH), dtype=bf, device=dev)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.shapes = {0: (self.B * G, G), 1: (self.B * G // 2, G // 2), 2: (self.B * G // 4, G // 4)}
+        g = self.g
+        self.shapes = {0: (self.B * g, g), 1: (self.B * g // 2, g // 2), 2: (self.B * g // 4, g // 4)}
         self.act = {}
         for name, lvl, *_r in LAYERS:
             r, c = self.shapes[lvl]
@@ -143,7 +145,7 @@ class Net:
 
     # ------------------------------------------------------------- forward
     def forward(self, x0, stream=None, tensor_cores=True):
-        """x0: BF16 [B*G, G, 32]; returns the FP32 output [B*G, G, 32] (channel 0)."""
+        """x0: BF16 [B*g, g, 32]; returns the FP32 output [B*g, g, 32] (channel 0)."""
         L = _lib()
         tc = 1 if tensor_cores else 0
         a = self.act
@@ -152,7 +154,7 @@ class Net:
         def conv(li, x, y, yf, lvl, up, skip, relu):
             r, c = self.shapes[lvl]
             _chk(L.fs_conv3x3(_p(x), _p(self.wpk[li]), _p(self.w(li)), _p(self.b(li)), _p(skip), _p(y), _p(yf), r, c,
-                              G >> lvl, int(up), int(relu), tc, _p(self.err), stream))
+                              self.g >> lvl, int(up), int(relu), tc, _p(self.err), stream))
 
         conv(0, x0, a["e1"], None, 0, False, None, True)
         _chk(L.fs_net_avgpool2(_p(a["e1"]), _p(self.pool1), *self.shapes[1], stream))
@@ -189,12 +191,13 @@ class Net:
             dz = torch.empty((r, c, CH), dtype=torch.float32, device=self.dev)
             dzb = torch.empty((r, c, CH), dtype=torch.bfloat16, device=self.dev)
             _chk(L.fs_net_relu_bwd(_p(da), _p(da2), _p(out_act), _p(dz), _p(dzb), n, int(relu), stream))
-            _chk(L.fs_net_weight_grad(_p(dz), _p(x_in), _p(gw(li)), _p(gb(li)), r, c, G >> lvl_out, int(up), stream))
+            _chk(L.fs_net_weight_grad(_p(dz), _p(x_in), _p(gw(li)), _p(gb(li)), r, c, self.g >> lvl_out, int(up),
+                                      stream))
             if not want_dx:
                 return None, dz
             dxh = torch.empty((r, c, CH), dtype=torch.float32, device=self.dev)
             _chk(L.fs_conv3x3(_p(dzb), _p(self.wflip_pk[li]), _p(self.wflip[li]), None, None, None, _p(dxh), r, c,
-                              G >> lvl_out, 0, 0, 1, _p(self.err), stream))
+                              self.g >> lvl_out, 0, 0, 1, _p(self.err), stream))
             if not up:
                 return dxh, dz
             lo = zeros(lvl_out + 1)
@@ -233,9 +236,9 @@ class Adam:
 
 
 def mse_loss(net: Net, target, stream=None):
-    """target: FP32 [B*G, G] coarse correction in network units. Returns (loss, dy)."""
+    """target: FP32 [B*g, g] coarse correction in network units. Returns (loss, dy)."""
     torch = net.torch
-    n = net.B * G * G
+    n = net.B * net.g * net.g
     dy = torch.empty_like(net.y)
     parts = torch.empty((n + 255) // 256, dtype=torch.float32, device=net.dev)
     _chk(_lib().fs_net_mse(_p(net.y), _p(target), _p(dy), _p(parts), n, stream))

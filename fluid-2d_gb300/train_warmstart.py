@@ -70,25 +70,31 @@ def _view(ptr, rows, pitch, device):
     return out
 
 
-def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 1024), device="cuda", log=None):
-    """Returns (X [S, G, G, 32] BF16 network inputs, T [S, G, G] FP32 targets, info).
-    Run k uses sweeps[k % len(sweeps)] pressure sweeps per projection."""
+def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 1024), g=None, device="cuda",
+             log=None, rmin=None, rmax=None, vortices=16):
+    """Returns (X [S, g, g, 32] BF16 network inputs, T [S, g, g] FP32 targets, info).
+    Run k uses sweeps[k % len(sweeps)] pressure sweeps per projection; g is the coarse
+    grid (default 32); vortex core radii default to size/100 .. size/25 cells."""
     torch = _torch()
     import fluid2d_gb300 as pkg
     from fluid2d_gb300 import workloads
 
+    g = g or G
+    kappa = g * g / 16.0
     L = pkg.load()
     Cm, lam = dct_basis(size, device)
-    R = size // G
+    R = size // g
+    rmin = size / 100.0 if rmin is None else rmin
+    rmax = size / 25.0 if rmax is None else rmax
     xs, ts = [], []
     scale = torch.zeros(1, dtype=torch.float32, device=device)
-    work = torch.zeros(G * G, dtype=torch.float32, device=device)
+    work = torch.zeros(g * g, dtype=torch.float32, device=device)
     run = 0
     t0 = time.time()
     while len(ts) < n_samples:
         kp = sweeps[run % len(sweeps)]
-        w = workloads.vortex_field(size, seed=seed + run, kd=20, kp=kp, dt=0.05, rate=1e-5, vortices=16,
-                                   rmin=size / 100.0, rmax=size / 25.0)
+        w = workloads.vortex_field(size, seed=seed + run, kd=20, kp=kp, dt=0.05, rate=1e-5, vortices=vortices,
+                                   rmin=rmin, rmax=rmax)
         s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=kp, warm_start=pkg.FS_WARM_PREVIOUS,
                        capture=1, check_finite=0, device=0)
         s.upload(*w.state())
@@ -99,11 +105,11 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 
             for slot in (0, 1):
                 dptr, sptr, fptr = s.capture_view(slot)
                 div = _view(dptr, w.rows, pitch, device)[1:-1, 1:size + 1].double()
-                pstar_c = neumann_solve(div, Cm, lam).reshape(G, R, G, R).mean(dim=(1, 3)).float()
+                pstar_c = neumann_solve(div, Cm, lam).reshape(g, R, g, R).mean(dim=(1, 3)).float()
                 for pptr in (sptr, fptr):
-                    xin = torch.zeros((G, G, 32), dtype=torch.bfloat16, device=device)
-                    pc = torch.zeros((G, G), dtype=torch.float32, device=device)
-                    rc = L.fs_net_restrict(C.c_void_p(dptr), C.c_void_p(pptr), w.rows, w.cols, pitch, G,
+                    xin = torch.zeros((g, g, 32), dtype=torch.bfloat16, device=device)
+                    pc = torch.zeros((g, g), dtype=torch.float32, device=device)
+                    rc = L.fs_net_restrict(C.c_void_p(dptr), C.c_void_p(pptr), w.rows, w.cols, pitch, g,
                                            C.c_void_p(work.data_ptr()), C.c_void_p(scale.data_ptr()),
                                            C.c_void_p(xin.data_ptr()), C.c_void_p(pc.data_ptr()), None)
                     if rc != 0:
@@ -111,7 +117,7 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 
                     corr = pstar_c - pc
                     corr = corr - corr.mean()
                     xs.append(xin)
-                    ts.append(corr / (scale * Lm.KAPPA))
+                    ts.append(corr / (scale * kappa))
                 if len(ts) >= n_samples:
                     break
             if len(ts) >= n_samples:
@@ -122,42 +128,62 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 
             log(f"generated {len(ts)} samples ({run} runs, {time.time() - t0:.1f} s)")
     X = torch.stack(xs[:n_samples])
     T = torch.stack(ts[:n_samples])
-    return X, T, {"runs": run, "size": size, "seconds": time.time() - t0, "sweeps": list(sweeps)}
+    return X, T, {"runs": run, "size": size, "g": g, "seconds": time.time() - t0, "sweeps": list(sweeps)}
 
 
 def train(X, T, epochs=4, batch=128, lr=1e-3, seed=0, log=None):
     """Trains the network on (X, T); returns (params as numpy, loss history)."""
+    return train_sets([(X, T)], epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
+
+
+def train_sets(sets, epochs=4, batch=128, lr=1e-3, seed=0, log=None):
+    """Trains one network on several data sets, possibly of different coarse grid sizes
+    ([(X, T), ...], X [S, g, g, 32]); batches of the sets are interleaved in a seeded
+    random order. Returns (params as numpy, loss history)."""
     torch = _torch()
-    dev = X.device
-    S = X.shape[0]
+    dev = sets[0][0].device
     params = torch.from_numpy(Lm.init_params(seed)).to(dev)
-    net = Lm.Net(B=batch, params=params)
-    opt = Lm.Adam(net, lr=lr)
-    g = torch.Generator(device="cpu").manual_seed(seed)
+    nets = {}
+    for X, _ in sets:
+        g = int(X.shape[1])
+        if g not in nets:
+            nets[g] = Lm.Net(B=batch, params=params, g=g)
+    first = next(iter(nets.values()))
+    opt = Lm.Adam(first, lr=lr)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
     hist = []
     for ep in range(epochs):
-        perm = torch.randperm(S, generator=g)
-        for b0 in range(0, S - batch + 1, batch):
-            idx = perm[b0:b0 + batch].to(dev)
-            x0 = X[idx].reshape(batch * G, G, 32).contiguous()
-            t = T[idx].reshape(batch * G, G).contiguous()
+        order = []
+        for si, (X, _) in enumerate(sets):
+            perm = torch.randperm(X.shape[0], generator=gen)
+            order += [(si, perm[b0:b0 + batch]) for b0 in range(0, X.shape[0] - batch + 1, batch)]
+        for k in torch.randperm(len(order), generator=gen).tolist():
+            si, idx = order[k]
+            X, T = sets[si]
+            g = int(X.shape[1])
+            net = nets[g]
+            net.repack()  # the shared parameters changed since this net last packed them
+            idx = idx.to(dev)
+            x0 = X[idx].reshape(batch * g, g, 32).contiguous()
+            t = T[idx].reshape(batch * g, g).contiguous()
             net.forward(x0)
             loss, dy = Lm.mse_loss(net, t)
             grad = net.backward(x0, dy)
             opt.step(grad)
             hist.append(float(loss))
         if log:
-            log(f"epoch {ep}: loss {np.mean(hist[-max(1, S // batch):]):.4e}")
+            log(f"epoch {ep}: loss {np.mean(hist[-max(1, len(order)):]):.4e}")
     return params.cpu().numpy(), hist
 
 
 def evaluate_loss(params, X, T, batch=128):
     torch = _torch()
-    net = Lm.Net(B=batch, params=torch.from_numpy(np.asarray(params, np.float32)).to(X.device))
+    g = int(X.shape[1])
+    net = Lm.Net(B=batch, params=torch.from_numpy(np.asarray(params, np.float32)).to(X.device), g=g)
     tot, n = 0.0, 0
     for b0 in range(0, X.shape[0] - batch + 1, batch):
-        x0 = X[b0:b0 + batch].reshape(batch * G, G, 32).contiguous()
-        t = T[b0:b0 + batch].reshape(batch * G, G).contiguous()
+        x0 = X[b0:b0 + batch].reshape(batch * g, g, 32).contiguous()
+        t = T[b0:b0 + batch].reshape(batch * g, g).contiguous()
         net.forward(x0)
         loss, _ = Lm.mse_loss(net, t)
         tot += float(loss)

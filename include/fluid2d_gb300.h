@@ -88,6 +88,7 @@ typedef struct fs_config {
                                   0 = as many as pressure_max_iterations allows. Steps stop at
                                   convergence (read on the host after each segment). */
     int learned_cycle_iterations; /* Jacobi sweeps after each correction; 0 = 128 */
+    int learned_grid;          /* coarse grid side of the network, 32 or 64; 0 = 32 */
 } fs_config;
 
 typedef struct fs_stats {
@@ -185,11 +186,13 @@ FS_API int fs_device_view_get(fs_solver* s, fs_device_view* out);
 
 /* Learned warm start (FS_WARM_LEARNED): load the network's FP32 parameters (8 layers x
  * (32x9x32 weights [co][tap][ci] + 32 biases) = FS_NET_PARAMS floats, host memory). The
- * grid must be square with an interior divisible by FS_NET_GRID. Each projection then
- * computes the divergence, runs the network on the FS_NET_GRID^2 coarse grid, adds the
- * interpolated correction to the previous pressure, and starts Jacobi from whichever of
- * that guess and the previous pressure has the smaller residual. */
+ * grid must be square with an interior divisible by FS_NET_GRID. The network runs on a
+ * G x G coarse grid (G = FS_NET_GRID or FS_NET_GRID_MAX, config learned_grid) on block
+ * sums of the pressure's residual; its correction
+ * is post-smoothed on the coarse grid, interpolated and added where it brings the
+ * pressure closer to the solution (see fs_config.learned_cycles). */
 #define FS_NET_GRID 32
+#define FS_NET_GRID_MAX 64
 #define FS_NET_PARAMS (8 * (32 * 9 * 32 + 32))
 FS_API int fs_set_network(fs_solver* s, const float* params, long long count);
 

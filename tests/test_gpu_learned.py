@@ -183,9 +183,10 @@ def _sweeps(fluid, w, warm, params, tol, steps=3, cap=20000):
 
 def test_trained_network_cuts_sweeps(fluid, wl):
     """What the trained network gains: the committed parameters (trained on the GPU by
-    `bench.py --workload learned --samples 20000 --epochs 12 --weights ...` on 512^2
-    runs) against the previous-pressure warm start and against an all-zero network
-    (coarse post-smoothing alone), on a 258^2 vortex field solved to a 5e-2 residual."""
+    `bench.py --workload learned --samples 20000 --epochs 12 --weights ...` on 512^2 and
+    1024^2 runs) against the previous-pressure warm start and against an all-zero
+    network (coarse post-smoothing alone), on a 258^2 vortex field solved to a 5e-2
+    residual."""
     params = np.load(GOLDEN / "warmstart_params.npy").astype(np.float32)
     w = wl.vortex_field(256, seed=8, kd=20, kp=20, dt=0.05, rate=1e-5, vortices=32, rmin=5, rmax=20)
     prev = _sweeps(fluid, w, fluid.FS_WARM_PREVIOUS, None, 5e-2)
