@@ -165,6 +165,9 @@ cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* b
                                  int G, int nu, const int* skip_if, cudaStream_t st);
 cudaError_t launch_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
                            const float* scale, float kappa, const int* skip_if, cudaStream_t st);
+// One damped (weight 1/2) Jacobi step of p into out, Neumann-filled edges (net.cu).
+cudaError_t launch_damp(const float* div, const float* p, float* out, int rows, int cols, int pitch,
+                        const int* skip_if, cudaStream_t st);
 cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float* p_try, int rows, int cols,
                                int pitch, double* out, const int* skip_if, cudaStream_t st);
 cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, long n_floats, const double* gain,

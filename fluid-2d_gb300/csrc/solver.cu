@@ -318,7 +318,8 @@ int enqueue_div_pass(fs_solver* s, const float* u_in, const float* v_in, Counter
 
 constexpr int kCoarseSweeps = 20;
 
-// One learned correction of p_cur (the current pressure, edges filled): the block sums
+// One learned correction of p_cur (the current pressure, edges filled): two damped
+// Jacobi steps (see launch_damp), then the block sums
 // of its residual on the coarse grid, the 8-layer network on the tensor cores, coarse
 // post-smoothing, bilinear interpolation into a candidate p_cur + correction; beside it
 // the classical candidate (the coarse smoothing from zero, no network). The judge keeps
@@ -327,6 +328,10 @@ constexpr int kCoarseSweeps = 20;
 // network's candidate won. Does nothing to p_cur once *converged (nullable) is set.
 int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged, Counter& cnt) {
     const int G = s->net.G;
+    // one damped Jacobi step first: removes the checkerboard error plain Jacobi never damps
+    CK(launch_damp(s->div, p_cur, s->p[0], s->rows, s->cols, s->pitch, converged, s->stream));
+    CK(launch_damp(s->div, s->p[0], p_cur, s->rows, s->cols, s->pitch, converged, s->stream));
+    cnt.launches += 2;
     const float kappa = net_kappa(G);
     CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
                               net_act(s, 0), converged, s->stream));
