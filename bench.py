@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--weights", default="", help="learned: save trained parameters here (.npy)")
     ap.add_argument("--load-weights", default="", help="learned: skip training and load parameters")
     ap.add_argument("--eval-sizes", default="1024,2048")
-    ap.add_argument("--tols", default="1e-1,3e-2,1e-2,1e-4")
+    ap.add_argument("--tols", default="1e-1,1e-2,1e-3,1e-4")
     ap.add_argument("--workload", choices=("vortex", "small", "batch", "residual", "learned", "gauss-seidel",
                                            "depth"),
                     default="vortex",
@@ -71,7 +71,8 @@ def parse():
                          "batch: 256 uneven grids, 30/30 sweeps, batch vs looped handles; "
                          "residual: pressure to a relative-residual target")
     ap.add_argument("--tol", type=float, default=1e-4)
-    ap.add_argument("--max-iters", type=int, default=2000)
+    ap.add_argument("--max-iters", type=int, default=None,
+                    help="sweep cap per projection (default: residual 2000, learned 20000, depth 400)")
     ap.add_argument("--count", type=int, default=256)
     ap.add_argument("--tune", action="store_true", help="autotune the tiling before timing")
     ap.add_argument("--cycles", type=int, default=0, help="learned: most corrections per projection (0 = cap / cycle-iters)")
@@ -759,6 +760,8 @@ def run_learned(a):
 
 def main():
     a = parse()
+    if a.max_iters is None:
+        a.max_iters = {"learned": 20000, "depth": 400}.get(a.workload, 2000)
     if a.warmup < 3:
         a.warmup = 3
     if a.impl == "reference":
