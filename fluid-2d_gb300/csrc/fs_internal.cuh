@@ -186,11 +186,12 @@ cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, f
                                    cudaStream_t st);
 
 // Gauss-Seidel compatibility step (gs.cu): the host solver's method, bit for bit, on a
-// square n x n grid of pitched fields; three scratch fields of the same shape.
+// square n x n grid of pitched fields; four scratch fields of the same shape.
 struct GsFields {
     float *d, *u, *v;
     const float *ds, *us, *vs;
-    float* scratch[3];
+    float* scratch[4];
+    float* aux;  // two floats of device scratch
 };
 int gs_max_size();                 // largest n on the current device
 cudaError_t gs_prepare();          // shared-memory opt-in on the current device, outside capture

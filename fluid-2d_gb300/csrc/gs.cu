@@ -13,13 +13,19 @@
 // flight at once. An edge cell is read only by its inner neighbour, so the thread that
 // updates that neighbour also rewrites the edge (the fill the host solver does after
 // every sweep); corners are never read by a sweep and are averaged once at the end.
-// The splat keeps raster order: the whole CTA computes the targets and weights of a
-// chunk of source cells, one thread then applies them in order.
+// The splat keeps the host solver's order of additions to every cell: a cell receives
+// its contributions in the raster order of their source cells. When no source moves
+// more than kGatherMaxD cells, each target cell gathers them itself, scanning the
+// sources around it in raster order (many CTAs); otherwise the whole CTA computes the
+// targets and weights of a chunk of source cells and one thread applies them in order.
 //
 // A step is four launches on the solver's pitched fields (element (i, j) at i*P + j):
-//   1. 3 CTAs: add sources + diffuse d | copy u, add sources, diffuse u | same for v
-//   2. 2 CTAs: splat d by the step's initial velocity (the copies) | project u, v
-//   3. 1 CTA : copy u, v; advect both by the copies (gather)
+//   1. 3 CTAs: add sources + diffuse d | copy u, add sources, diffuse u, largest
+//      displacement | same for v
+//   2. project u, v (CTA 0) | splat d by the step's initial velocity into a scratch
+//      field: one CTA in order (CTA 1) or one CTA per 1024 target cells (CTAs 2..)
+//   3. copy u, v and advect both by the copies (CTA 0) | the splat result and the
+//      host solver's fill into d (CTA 1)
 //   4. 1 CTA : project u, v
 // Every operation uses explicitly rounded single-precision intrinsics so that no
 // contraction changes a result; the outputs are bit-identical to the host solver's.
@@ -33,7 +39,8 @@ namespace fs {
 namespace {
 
 constexpr int kGsThreads = 1024;
-constexpr int kGsStage = 512;  // source cells per splat chunk
+constexpr int kGsStage = 512;   // source cells per splat chunk (in-order path)
+constexpr int kGatherMaxD = 16; // largest displacement (cells) for the gathering splat
 
 struct GsStageEntry {
     int i0, j0;
@@ -113,6 +120,8 @@ struct GsArgs {
     float* su;           // scratch: copy of u
     float* sv;           // scratch: copy of v
     float* dv;           // scratch: divergence
+    float* acc;          // scratch: splat result (interior)
+    float* dmax;         // scratch: largest |dt0 u| and |dt0 v| of the step's initial velocity
     int n, P, kd, kp;
     float a[3], den[3];  // diffusion constants per field
     float dt, dt0, h;
@@ -160,7 +169,7 @@ __device__ void gs_splat(const GsArgs& A, float* acc, GsStageEntry* stage) {
             const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
             const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
             GsStageEntry en;
-            if (x < 0.5f || x > hi || y < 0.5f || y > hi) {
+            if (!(x >= 0.5f && x <= hi && y >= 0.5f && y <= hi)) {  // NaN-safe form of the skip test
                 en.i0 = -1;
                 en.j0 = 0;
                 en.w[0] = en.w[1] = en.w[2] = en.w[3] = 0.f;
@@ -192,8 +201,41 @@ __device__ void gs_splat(const GsArgs& A, float* acc, GsStageEntry* stage) {
         }
     }
     __syncthreads();
-    cpu_fill(acc, n, n, BND_CONT);
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A.f[0][(e / n) * P + e % n] = acc[e];
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int i = 1 + e / m, j = 1 + e % m;
+        A.acc[i * P + j] = acc[i * n + j];
+    }
+}
+
+// The same splat gathered by target: thread t of target block b owns interior cell
+// T = b*blockDim + t and adds, in the raster order of the sources, the contribution of
+// every source within W = D + 2 cells (D = the largest displacement, so every source
+// that can reach T is scanned); each source reaches T through at most one corner.
+__device__ void gs_splat_gather(const GsArgs& A, int b, int D) {
+    const int n = A.n, P = A.P, m = n - 2;
+    const int e = b * blockDim.x + threadIdx.x;
+    if (e >= m * m) return;
+    const int ti = 1 + e / m, tj = 1 + e % m;
+    const float hi = (float)n - 1.5f;
+    const float* d0 = A.f[0];
+    const int W = D + 2;
+    const int i_lo = max(1, ti - W), i_hi = min(n - 2, ti + W), j_lo = max(1, tj - W), j_hi = min(n - 2, tj + W);
+    float acc = 0.f;
+    for (int i = i_lo; i <= i_hi; ++i)
+        for (int j = j_lo; j <= j_hi; ++j) {
+            const int o = i * P + j;
+            const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
+            const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
+            if (!(x >= 0.5f && x <= hi && y >= 0.5f && y <= hi)) continue;
+            const int j0 = (int)x, i0 = (int)y;
+            const int di = ti - i0, dj = tj - j0;  // which corner of the source's cell T is
+            if ((unsigned)di > 1u || (unsigned)dj > 1u) continue;
+            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+            const float wy = di ? s2 : s3, wx = dj ? s0 : s1;
+            acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(wx, wy), d0[o]));
+        }
+    A.acc[ti * P + tj] = acc;
 }
 
 // project (fluid_solver_cpu.cpp:179-215) of (u, v), pressure from zero in shared memory.
@@ -260,7 +302,26 @@ __global__ void __launch_bounds__(kGsThreads) gs_diffuse_kernel(const __grid_con
     float* x = reinterpret_cast<float*>(gs_smem);
     const int k = blockIdx.x;
     if (k > 0) {  // keep the step's initial velocity for the density splat
-        copy_field(k == 1 ? A.su : A.sv, A.f[k], A.n, A.P);
+        float* dst = k == 1 ? A.su : A.sv;
+        const float* src = A.f[k];
+        const int n = A.n, P = A.P, m = n - 2;
+        copy_field(dst, src, n, P);
+        // largest interior displacement |dt0 * velocity| (non-finite counts as huge)
+        float dm = 0.f;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            float a = fabsf(__fmul_rn(A.dt0, src[(1 + e / m) * P + 1 + e % m]));
+            if (!(a <= 1e30f)) a = 1e30f;
+            dm = fmaxf(dm, a);
+        }
+        __shared__ float red[32];
+        for (int o = 16; o > 0; o >>= 1) dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float t = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
+            A.dmax[k - 1] = t;
+        }
         __syncthreads();
     }
     gs_diffuse(A, k, x);
@@ -269,13 +330,33 @@ __global__ void __launch_bounds__(kGsThreads) gs_diffuse_kernel(const __grid_con
 __global__ void __launch_bounds__(kGsThreads) gs_splat_project_kernel(const __grid_constant__ GsArgs A) {
     extern __shared__ float4 gs_smem[];
     float* f = reinterpret_cast<float*>(gs_smem);
+    // every CTA reads the same two values (written by the previous launch)
+    const float dm = fmaxf(__ldcg(A.dmax), __ldcg(A.dmax + 1));
+    const bool gather = dm <= (float)kGatherMaxD;
     if (blockIdx.x == 0)
-        gs_splat(A, f, reinterpret_cast<GsStageEntry*>(f + A.n * A.n));
-    else
         gs_project(A, f);
+    else if (blockIdx.x == 1) {
+        if (!gather) gs_splat(A, f, reinterpret_cast<GsStageEntry*>(f + A.n * A.n));
+    } else if (gather) {
+        gs_splat_gather(A, blockIdx.x - 2, (int)ceilf(dm));
+    }
 }
 
-__global__ void __launch_bounds__(kGsThreads) gs_gather_kernel(const __grid_constant__ GsArgs A) { gs_gather(A); }
+// CTA 0: advect u, v; CTA 1: density = the splat result with the host solver's fill.
+__global__ void __launch_bounds__(kGsThreads) gs_gather_kernel(const __grid_constant__ GsArgs A) {
+    if (blockIdx.x == 0) {
+        gs_gather(A);
+        return;
+    }
+    const int n = A.n, P = A.P, m = n - 2;
+    float* d = A.f[0];
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int o = (1 + e / m) * P + 1 + e % m;
+        d[o] = A.acc[o];
+    }
+    __syncthreads();
+    cpu_fill(d, n, P, BND_CONT);
+}
 
 __global__ void __launch_bounds__(kGsThreads) gs_project_kernel(const __grid_constant__ GsArgs A) {
     extern __shared__ float4 gs_smem[];
@@ -322,6 +403,8 @@ cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float d
     A.su = F.scratch[0];
     A.sv = F.scratch[1];
     A.dv = F.scratch[2];
+    A.acc = F.scratch[3];
+    A.dmax = F.aux;
     A.n = n;
     A.P = pitch;
     A.kd = kd;
@@ -339,8 +422,9 @@ cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float d
     A.h = 1.0f / sqrtf(cells);
     const size_t smem = gs_smem_bytes(n);
     gs_diffuse_kernel<<<3, kGsThreads, smem, st>>>(A);
-    gs_splat_project_kernel<<<2, kGsThreads, smem, st>>>(A);
-    gs_gather_kernel<<<1, kGsThreads, 0, st>>>(A);
+    const int target_blocks = ((n - 2) * (n - 2) + kGsThreads - 1) / kGsThreads;
+    gs_splat_project_kernel<<<2 + target_blocks, kGsThreads, smem, st>>>(A);
+    gs_gather_kernel<<<2, kGsThreads, 0, st>>>(A);
     gs_project_kernel<<<1, kGsThreads, smem, st>>>(A);
     return cudaGetLastError();
 }

@@ -645,6 +645,8 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
         F.us = s->src[F_U];
         F.vs = s->src[F_V];
         for (int k = 0; k < 3; ++k) F.scratch[k] = s->x0[k];
+        F.scratch[3] = s->acc;
+        F.aux = s->div;  // unused by this method
         CK(gs_step(F, s->rows, s->pitch, s->cfg.diffuse_iterations, s->cfg.pressure_iterations, diff, visc, dt,
                    s->stream));
         cnt.launches += 4;
