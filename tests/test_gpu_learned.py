@@ -59,20 +59,6 @@ def test_forward_and_gradients_match_cpu_reference(fluid):
     assert np.all(grad[~live] == 0.0)
 
 
-def test_exact_neumann_solve_is_the_jacobi_fixed_point(wl):
-    import torch
-
-    _, T = _mods()
-    n = 24
-    _, u, v, _, _, _ = wl.random_state(n + 2, n + 2, 9, vmax=1.0)
-    wl.reflect_boundaries(u, v)
-    _, _, p_jac, div = oracle.project(u, v, 30000, f64=True)
-    Cm, lam = T.dct_basis(n, "cpu")
-    p = T.neumann_solve(torch.from_numpy(div[1:-1, 1:-1]), Cm, lam).numpy()
-    pj = p_jac[1:-1, 1:-1] - p_jac[1:-1, 1:-1].mean()
-    assert np.abs(p - pj).max() <= 1e-6 * np.abs(pj).max()
-
-
 def test_training_reduces_the_loss(fluid):
     _, T = _mods()
     X, Y, info = T.generate(256, size=128, steps_per_run=64, seed=7)

@@ -139,6 +139,15 @@ def test_vortex_field_steps(fluid, wl):
     assert max(worst) <= TOL, worst
 
 
+@pytest.mark.parametrize("n,steps", [(2048, 2), (4096, 1)])
+def test_benchmark_size_steps(fluid, wl, n, steps):
+    """The benchmark's own workload at its full size (vortex field, Kd = Kp = 40, dt 0.05,
+    rates 1e-5) and at twice it, against the oracle step by step."""
+    w = wl.vortex_field(n, seed=2, kd=40, kp=40)
+    worst, st = _run_lockstep(fluid, w, steps, 40, 40)
+    assert max(worst) <= TOL, worst
+
+
 def test_non_square(fluid, wl):
     rows, cols = 47, 90
     d, u, v, ds, us, vs = rand(wl, rows, cols, 12, vmax=0.02)
