@@ -78,6 +78,7 @@ def parse():
     ap.add_argument("--cycles", type=int, default=0, help="learned: most corrections per projection (0 = cap / cycle-iters)")
     ap.add_argument("--cycle-iters", type=int, default=256, help="learned: Jacobi sweeps after each correction")
     ap.add_argument("--train-size", type=int, default=512, help="learned: grid of the training runs")
+    ap.add_argument("--learned-grid", type=int, default=0, help="learned: coarse grid side (0 = default, 32, 64)")
     return ap.parse_args()
 
 
@@ -715,7 +716,8 @@ def run_learned(a):
             for mode, warm, net_params in modes:
                 s = pkg.Solver(w.rows, w.cols, diffuse_iterations=a.kd, pressure_tolerance=tol,
                                pressure_max_iterations=a.max_iters, warm_start=warm, device=0, check_finite=0,
-                               learned_cycles=a.cycles, learned_cycle_iterations=a.cycle_iters)
+                               learned_cycles=a.cycles, learned_cycle_iterations=a.cycle_iters,
+                               learned_grid=a.learned_grid)
                 if warm == pkg.FS_WARM_LEARNED:
                     s.set_network(net_params)
                 s.upload(*w.state())

@@ -13,12 +13,13 @@
 // (add_sources for diffusion, the divergence for pressure) and the last pressure
 // pass fuses the gradient subtract and the two reflecting fills.
 //
-// Each thread owns one column of SR consecutive rows and keeps its current values
-// and its constant term (x0 or div) in registers; neighbours come from the shared
-// copy of the previous sweep (double-buffered, one barrier per sweep, a second one
-// only in CTAs whose region touches a domain edge). All arithmetic uses explicit
-// round-to-nearest intrinsics in the reference's operand order, so no FMA
-// contraction changes its rounding. The reference divides by (1.0 + 4.0*a) in
+// Each thread owns one column of SR consecutive rows and keeps its constant terms
+// (x0 or div) in registers; every sweep streams down the column from the shared copy
+// of the previous sweep (double-buffered, one barrier per sweep, a second one only in
+// CTAs whose region touches a domain edge) as two rolling windows in lockstep, so
+// each pair of cell updates issues as packed f32x2 instructions. All arithmetic uses
+// explicit round-to-nearest intrinsics in the reference's operand order, so no FMA
+// contraction changes its rounding (the one multiply feeding an add stays scalar). The reference divides by (1.0 + 4.0*a) in
 // double; FP64 is slow on GB300, so the quotient is formed as
 //   q = num*rf;  e = fma(-q, dh, num);  e = fma(-q, dl, e);  q = fma(e, rf, q)
 // with dh + dl = 1 + 4a split into two floats and rf = (float)(1/(1 + 4a)). This
