@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--count", type=int, default=256)
     ap.add_argument("--tune", action="store_true", help="autotune the tiling before timing")
     ap.add_argument("--cycles", type=int, default=0, help="learned: most corrections per projection (0 = cap / cycle-iters)")
-    ap.add_argument("--cycle-iters", type=int, default=256, help="learned: Jacobi sweeps after each correction")
+    ap.add_argument("--cycle-iters", type=int, default=128, help="learned: Jacobi sweeps after each correction")
     ap.add_argument("--train-size", type=int, default=512, help="learned: grid of the training runs")
     ap.add_argument("--learned-grid", type=int, default=0, help="learned: coarse grid side (0 = default, 32, 64)")
     return ap.parse_args()
