@@ -163,6 +163,14 @@ cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, i
                                    double* norm2, float* scale, void* xin, const int* skip_if, cudaStream_t st);
 cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* bs, const float* scale, float kappa,
                                  int G, int nu, const int* skip_if, cudaStream_t st);
+// The network input (channel 0 = bs / RMS(bs), scale, norm) from given block sums.
+cudaError_t launch_coarse_input(const float* bs, int G, float* scale, void* xin, double* norm2, const int* skip_if,
+                                cudaStream_t st);
+// Block sums on G x G from those on 2G x 2G; a G x G correction (channel 0 times
+// scale*kappa) interpolated onto 2G x 2G in absolute units (channel-0 stride 32).
+cudaError_t launch_coarse_sum2x2(const float* fine, float* coarse, int G, const int* skip_if, cudaStream_t st);
+cudaError_t launch_coarse_interp(const float* y, float* e, int G, const float* scale, float kappa,
+                                 const int* skip_if, cudaStream_t st);
 cudaError_t launch_prolong(const float* y, const float* p_prev, float* p_out, int rows, int cols, int pitch, int G,
                            const float* scale, float kappa, const int* skip_if, cudaStream_t st);
 // One damped (weight 1/2) Jacobi step of p into out, Neumann-filled edges (net.cu).

@@ -382,6 +382,40 @@ __global__ void damp_kernel(const float* __restrict__ div, const float* __restri
     out[o] = damped_cell(div, p, (size_t)si * pitch + sj, pitch);
 }
 
+// Block sums on a G x G grid from those on the 2G x 2G grid (sum of the four children).
+__global__ void coarse_sum2x2_kernel(const float* __restrict__ fine, float* __restrict__ coarse, int G,
+                                     const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    const int G2 = 2 * G;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < G * G; c += gridDim.x * blockDim.x) {
+        const int I = c / G, J = c % G;
+        const float* f = fine + (size_t)(2 * I) * G2 + 2 * J;
+        coarse[c] = (f[0] + f[1]) + (f[G2] + f[G2 + 1]);
+    }
+}
+
+// A coarse correction on the G x G grid (channel 0 of y, times scale * kappa) carried
+// to the 2G x 2G grid by bilinear interpolation at the finer cell centres, in absolute
+// units, into channel 0 of e (stride 32, the layout the smoothing and prolongation use).
+__global__ void coarse_interp_kernel(const float* __restrict__ y, float* __restrict__ e, int G,
+                                     const float* __restrict__ scale_ptr, float kappa,
+                                     const int* __restrict__ skip_if) {
+    if (skip_if && __ldcg(skip_if)) return;
+    const int G2 = 2 * G;
+    const float unit = (*scale_ptr) * kappa;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < G2 * G2; c += gridDim.x * blockDim.x) {
+        const int I = c / G2, J = c % G2;
+        const float fy = (I + 0.5f) * 0.5f - 0.5f, fx = (J + 0.5f) * 0.5f - 0.5f;
+        const int y0 = max(0, min(G - 1, (int)floorf(fy))), x0 = max(0, min(G - 1, (int)floorf(fx)));
+        const int y1 = min(G - 1, y0 + 1), x1 = min(G - 1, x0 + 1);
+        const float wy = fminf(fmaxf(fy - y0, 0.f), 1.f), wx = fminf(fmaxf(fx - x0, 0.f), 1.f);
+        const float c00 = y[((size_t)y0 * G + x0) * kC], c01 = y[((size_t)y0 * G + x1) * kC];
+        const float c10 = y[((size_t)y1 * G + x0) * kC], c11 = y[((size_t)y1 * G + x1) * kC];
+        const float v = (1.f - wy) * ((1.f - wx) * c00 + wx * c01) + wy * ((1.f - wx) * c10 + wx * c11);
+        e[(size_t)c * kC] = v * unit;
+    }
+}
+
 // Keep the candidate with the largest positive energy gain (see launch_accept_best).
 __global__ void accept_best_kernel(float* __restrict__ p_cur, const float* __restrict__ pa,
                                    const float* __restrict__ pb, long n4, const double* __restrict__ gain,
@@ -409,6 +443,23 @@ cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, i
     const int R = (rows - 2) / G;
     restrict_kernel<<<G * G, 256, 0, st>>>(div, p, pitch, R, G, bs, nullptr, skip_if);
     coarse_input_kernel<<<1, 1024, 0, st>>>(bs, G, scale, (__nv_bfloat16*)xin, norm2, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_input(const float* bs, int G, float* scale, void* xin, double* norm2, const int* skip_if,
+                                cudaStream_t st) {
+    coarse_input_kernel<<<1, 1024, 0, st>>>(bs, G, scale, (__nv_bfloat16*)xin, norm2, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_sum2x2(const float* fine, float* coarse, int G, const int* skip_if, cudaStream_t st) {
+    coarse_sum2x2_kernel<<<(G * G + 255) / 256, 256, 0, st>>>(fine, coarse, G, skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_interp(const float* y, float* e, int G, const float* scale, float kappa,
+                                 const int* skip_if, cudaStream_t st) {
+    coarse_interp_kernel<<<(4 * G * G + 255) / 256, 256, 0, st>>>(y, e, G, scale, kappa, skip_if);
     return cudaGetLastError();
 }
 

@@ -117,7 +117,15 @@ struct fs_solver {
         double* res = nullptr;            // [coarse residual norm^2, energy gain: network, coarse only]
         float* bs = nullptr;              // coarse residual block sums of the current pressure, G*G
         float* yc = nullptr;              // coarse-only correction, G*G*32 (channel 0 used)
-        int G = FS_NET_GRID;              // coarse grid side (32 or 64)
+        int G = FS_NET_GRID;              // coarse grid side of the network (32 or 64)
+        // second, finer coarse level (2G x 2G) on large grids: block sums and the two
+        // candidates' corrections in absolute units, channel-0 stride 32; null when unused
+        int G2 = 0;
+        float* bs2 = nullptr;
+        float* e2a = nullptr;
+        float* e2b = nullptr;
+        float* scale2 = nullptr;
+        float* one = nullptr;             // device 1.0f (absolute units)
         void* mem = nullptr;
     } net;
     float* pguess = nullptr;  // fine starting pressure built from the network
@@ -316,7 +324,8 @@ int enqueue_div_pass(fs_solver* s, const float* u_in, const float* v_in, Counter
     return FS_OK;
 }
 
-constexpr int kCoarseSweeps = 20;
+constexpr int kCoarseSweeps = 20;       // on the network's grid
+constexpr int kCoarseSweepsFine = 200;  // on the finer coarse level
 
 // One learned correction of p_cur (the current pressure, edges filled): two damped
 // Jacobi steps (see launch_damp), then the block sums
@@ -333,9 +342,19 @@ int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged,
     CK(launch_damp(s->div, s->p[0], p_cur, s->rows, s->cols, s->pitch, converged, s->stream));
     cnt.launches += 2;
     const float kappa = net_kappa(G);
-    CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
-                              net_act(s, 0), converged, s->stream));
-    cnt.launches += 2;
+    const int G2 = s->net.G2;
+    if (G2) {
+        // block sums on the finer level, summed up for the network's level
+        CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G2, s->net.bs2, nullptr, s->net.scale2,
+                                  nullptr, converged, s->stream));
+        CK(launch_coarse_sum2x2(s->net.bs2, s->net.bs, G, converged, s->stream));
+        CK(launch_coarse_input(s->net.bs, G, s->net.scale, net_act(s, 0), s->net.res, converged, s->stream));
+        cnt.launches += 4;
+    } else {
+        CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
+                                  net_act(s, 0), converged, s->stream));
+        cnt.launches += 2;
+    }
     int rc;
     auto conv = [&](int li, int in, int out, int lvl, int up, int skip, int relu, float* yf) {
         const int g = G >> lvl;
@@ -362,10 +381,25 @@ int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged,
                             s->stream));
     CK(launch_coarse_smooth(nullptr, s->net.yc, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
                             s->stream));
-    CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
-                      s->stream));
-    CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
-                      s->stream));
+    if (G2) {
+        // both candidates continue on the finer coarse level, then go to the fine grid
+        CK(launch_coarse_interp(s->net.y, s->net.e2a, G, s->net.scale, kappa, converged, s->stream));
+        CK(launch_coarse_interp(s->net.yc, s->net.e2b, G, s->net.scale, kappa, converged, s->stream));
+        CK(launch_coarse_smooth(s->net.e2a, s->net.e2a, s->net.bs2, s->net.one, 1.f, G2, kCoarseSweepsFine, converged,
+                                s->stream));
+        CK(launch_coarse_smooth(s->net.e2b, s->net.e2b, s->net.bs2, s->net.one, 1.f, G2, kCoarseSweepsFine, converged,
+                                s->stream));
+        CK(launch_prolong(s->net.e2a, p_cur, s->pguess, s->rows, s->cols, s->pitch, G2, s->net.one, 1.f, converged,
+                          s->stream));
+        CK(launch_prolong(s->net.e2b, p_cur, pb, s->rows, s->cols, s->pitch, G2, s->net.one, 1.f, converged,
+                          s->stream));
+        cnt.launches += 4;
+    } else {
+        CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
+                          s->stream));
+        CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
+                          s->stream));
+    }
     CK(cudaMemsetAsync(s->net.res + 1, 0, 2 * sizeof(double), s->stream));
     CK(launch_energy_gain(s->div, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
     CK(launch_energy_gain(s->div, p_cur, pb, s->rows, s->cols, s->pitch, s->net.res + 2, converged, s->stream));
@@ -990,10 +1024,15 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         // network and the coarse smoothing both capture the smooth ones less well there)
         s->net.G = cfg->learned_grid > 0 ? cfg->learned_grid : FS_NET_GRID;
         const int G = s->net.G;
+        // the finer coarse level: 2G when the interior allows blocks of 16 cells or more
+        const int N = cfg->rows - 2;
+        s->net.G2 = (2 * G <= kNetGMax && N % (2 * G) == 0 && N / (2 * G) >= 16) ? 2 * G : 0;
+        const int G2 = s->net.G2;
         size_t acts = 0;
         for (int k = 0; k < kNetActs; ++k) acts += net_act_pixels(k, G) * kNetC;
         const size_t bytes = (size_t)FS_NET_PARAMS * 4 + 8 * 9216 * 2 + acts * 2 + (size_t)G * G * kNetC * 4 +
-                             256 * 4 + 2 * (size_t)G * G * 4 + (size_t)G * G * kNetC * 4;
+                             256 * 4 + 2 * (size_t)G * G * 4 + (size_t)G * G * kNetC * 4 +
+                             (size_t)G2 * G2 * 4 + 2 * (size_t)G2 * G2 * kNetC * 4;
         if ((e = cudaMalloc(&s->net.mem, bytes)) != cudaSuccess || (e = cudaMemset(s->net.mem, 0, bytes)) != cudaSuccess) {
             rc = cuda_fail(e, "fs_create: network buffers");
         } else {
@@ -1010,8 +1049,19 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
             s->net.counters = reinterpret_cast<unsigned long long*>(q + 32);    // 2
             s->net.scale = reinterpret_cast<float*>(q + 48);
             s->net.err = reinterpret_cast<int*>(q + 52);
+            s->net.scale2 = reinterpret_cast<float*>(q + 56);
+            s->net.one = reinterpret_cast<float*>(q + 60);
             s->net.bs = reinterpret_cast<float*>(q + 256 * 4);
             s->net.yc = s->net.bs + 2 * (size_t)G * G;
+            float* tail = s->net.yc + (size_t)G * G * kNetC;
+            if (G2) {
+                s->net.bs2 = tail;
+                s->net.e2a = s->net.bs2 + (size_t)G2 * G2;
+                s->net.e2b = s->net.e2a + (size_t)G2 * G2 * kNetC;
+            }
+            const float one = 1.f;
+            if ((e = cudaMemcpy(s->net.one, &one, sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+                rc = cuda_fail(e, "fs_create: network constants");
         }
     }
     if (rc == FS_OK && learned && (e = cudaMallocHost(&s->host_ctrl, sizeof(SolveCtrl))) != cudaSuccess)
