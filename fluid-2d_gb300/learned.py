@@ -12,11 +12,12 @@ of the correction e that solves the residual equation (4e - sum(nbrs e) = r), wh
 interpolated bilinearly back to the fine grid and added to p. The coarse problem has the
 same units at every fine size that G divides, so one network serves them all.
 
-In a fixed-count solve the network corrects the previous pressure once and the solver
-keeps whichever of the two starts has the lower residual. In a solve to a residual
-target the network corrects the current pressure before each segment of Jacobi
-sweeps, and the segment's first pass runs from both the corrected and the uncorrected
-pressure and keeps the better, so a correction that does not help costs one pass.
+The solver corrects the previous pressure once before a fixed-count solve, and the
+current pressure before every segment of Jacobi sweeps of a solve to a residual target.
+Each correction offers two candidates, the network's (post-smoothed on the coarse grid)
+and the coarse smoothing alone, and keeps the one that brings the pressure closest to
+the solution in the A-norm, or neither. On 1024^2 and larger grids both candidates are
+refined on a second, 64x64 coarse level before they reach the fine grid.
 
 Architecture (8 conv layers, 3x3, 32 channels, BF16 operands, FP32 accumulation; two
 average-pool downsamples and two nearest upsamples with additive skips):
