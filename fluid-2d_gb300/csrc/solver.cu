@@ -331,7 +331,7 @@ constexpr int kCoarseSweepsFine = 200;  // on the finer coarse level
 // Jacobi steps (see launch_damp), then the block sums
 // of its residual on the coarse grid, the 8-layer network on the tensor cores, coarse
 // post-smoothing, bilinear interpolation into a candidate p_cur + correction; beside it
-// the classical candidate (the coarse smoothing from zero, no network). The judge keeps
+// the classical candidate (the coarse smoothing from zero, no network). The acceptance rule keeps
 // the candidate that brings p_cur closest to the solution in the A-norm (the norm the
 // Jacobi iteration contracts), or p_cur when neither gets closer, and counts whether the
 // network's candidate won. Does nothing to p_cur once *converged (nullable) is set.

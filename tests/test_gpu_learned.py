@@ -111,7 +111,7 @@ def test_learned_cycles_reach_the_target_and_keep_parity(fluid, wl, trained):
     """Residual-target projections with network corrections: every projection meets the
     target (the residual of the pressure it ended with, recomputed by the oracle), and
     the step equals the oracle's step that projects with those final pressures. With
-    untrained weights the judge rejects the corrections and the solve still converges."""
+    untrained weights the acceptance rule rejects the corrections and the solve still converges."""
     Lm, T = _mods()
     if trained:
         X, Y, _ = T.generate(512, size=128, steps_per_run=32, seed=21, sweeps=(32, 128))
