@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--cycle-iters", type=int, default=128, help="learned: Jacobi sweeps after each correction")
     ap.add_argument("--train-size", type=int, default=512, help="learned: grid of the training runs")
     ap.add_argument("--learned-grid", type=int, default=0, help="learned: coarse grid side (0 = default, 32, 64)")
+    ap.add_argument("--mid-solve-samples", type=int, default=0,
+                    help="learned: add this many mid-solve states met by a first-round network, then retrain")
     return ap.parse_args()
 
 
@@ -693,18 +695,27 @@ def run_learned(a):
         X1, T1, g1 = train_warmstart.generate(half, size=a.train_size, steps_per_run=100, seed=100, g=32)
         X2, T2, g2 = train_warmstart.generate(a.samples - half, size=2 * a.train_size, steps_per_run=50, seed=500,
                                               g=32, rmin=20.0, rmax=80.0, vortices=64)
+        sets = [(X1, T1), (X2, T2)]
+        if a.mid_solve_samples:
+            # second round: states in the middle of learned solves, met with the first round's
+            # network, added to the data and the network trained again from scratch
+            p0, _ = train_warmstart.train_sets(sets, epochs=a.epochs, batch=128, lr=1e-3, seed=0)
+            X3, T3, _ = train_warmstart.generate(a.mid_solve_samples, size=2 * a.train_size, steps_per_run=25,
+                                                 seed=900, g=32, rmin=20.0, rmax=80.0, vortices=64, params=p0)
+            sets.append((X3, T3))
         t1 = time.perf_counter()
-        params, hist = train_warmstart.train_sets([(X1, T1), (X2, T2)], epochs=a.epochs, batch=128, lr=1e-3, seed=0)
+        params, hist = train_warmstart.train_sets(sets, epochs=a.epochs, batch=128, lr=1e-3, seed=0)
         t2 = time.perf_counter()
         base = [train_warmstart.evaluate_loss(learned.init_params(0), X[:2048], T[:2048]) for X, T in ((X1, T1), (X2, T2))]
         fin = [train_warmstart.evaluate_loss(params, X[:2048], T[:2048]) for X, T in ((X1, T1), (X2, T2))]
         info = {"samples": [int(X1.shape[0]), int(X2.shape[0])], "train_sizes": [a.train_size, 2 * a.train_size],
                 "coarse_grids": [32, 32], "gen_s": t1 - t0, "train_s": t2 - t1, "epochs": a.epochs,
                 "generation_sweeps": g1["sweeps"], "loss_init": base, "loss_trained": fin,
-                "loss_first_batch": hist[0], "loss_last_batch": hist[-1]}
+                "loss_first_batch": hist[0], "loss_last_batch": hist[-1],
+                "mid_solve_samples": a.mid_solve_samples}
         if a.weights:
             np.save(a.weights, params)
-        del X1, T1, X2, T2
+        del X1, T1, X2, T2, sets
         torch.cuda.empty_cache()
     results = []
     for size in [int(x) for x in a.eval_sizes.split(",")]:

@@ -71,10 +71,14 @@ def _view(ptr, rows, pitch, device):
 
 
 def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 1024), g=None, device="cuda",
-             log=None, rmin=None, rmax=None, vortices=16):
+             log=None, rmin=None, rmax=None, vortices=16, params=None, cycles=(2, 4, 8, 16)):
     """Returns (X [S, g, g, 32] BF16 network inputs, T [S, g, g] FP32 targets, info).
     Run k uses sweeps[k % len(sweeps)] pressure sweeps per projection; g is the coarse
-    grid (default 32); vortex core radii default to size/100 .. size/25 cells."""
+    grid (default 32); vortex core radii default to size/100 .. size/25 cells.
+
+    With `params`, the runs use the learned corrections themselves (those parameters, 128
+    sweeps per cycle) stopped after cycles[k % len(cycles)] cycles, so the final pressures
+    are the states the network meets in the middle of a solve."""
     torch = _torch()
     import fluid2d_gb300 as pkg
     from fluid2d_gb300 import workloads
@@ -95,13 +99,24 @@ def generate(n_samples, size=512, steps_per_run=100, seed=100, sweeps=(64, 256, 
         kp = sweeps[run % len(sweeps)]
         w = workloads.vortex_field(size, seed=seed + run, kd=20, kp=kp, dt=0.05, rate=1e-5, vortices=vortices,
                                    rmin=rmin, rmax=rmax)
-        s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=kp, warm_start=pkg.FS_WARM_PREVIOUS,
-                       capture=1, check_finite=0, device=0)
+        if params is None:
+            s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, pressure_iterations=kp,
+                           warm_start=pkg.FS_WARM_PREVIOUS, capture=1, check_finite=0, device=0)
+        else:
+            k = cycles[run % len(cycles)]
+            s = pkg.Solver(w.rows, w.cols, diffuse_iterations=20, warm_start=pkg.FS_WARM_LEARNED, capture=1,
+                           check_finite=0, device=0, pressure_tolerance=1e-9, pressure_max_iterations=128 * k,
+                           learned_cycle_iterations=128, learned_cycles=k)
+            s.set_network(np.asarray(params, np.float32))
         s.upload(*w.state())
         s.upload_sources(*w.sources())
         pitch = s.device_view().pitch
         for _ in range(steps_per_run):
-            s.step(w.diffusion, w.viscosity, w.dt, 1)
+            try:
+                s.step(w.diffusion, w.viscosity, w.dt, 1)
+            except pkg.FluidError as e:
+                if e.code != pkg.FS_ERR_NOT_CONVERGED:
+                    raise
             for slot in (0, 1):
                 dptr, sptr, fptr = s.capture_view(slot)
                 div = _view(dptr, w.rows, pitch, device)[1:-1, 1:size + 1].double()
