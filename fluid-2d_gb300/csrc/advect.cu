@@ -140,8 +140,11 @@ __global__ void __launch_bounds__(256) advect_velocity_kernel(const float* __res
 }
 
 // ----------------------------------------------------------------- batched
-// One launch covers every grid of a batch: blocks of 32x8 cells are numbered grid by
-// grid (prefix[g] = first block of grid g, block_job[b] = grid of block b).
+// One launch covers every grid of a batch: blocks of 32x8 threads each cover 32x32
+// cells (four rows per thread, so a large grid needs a quarter of the blocks one cell
+// per thread would), numbered grid by grid (prefix[g] = first block of grid g,
+// block_job[b] = grid of block b).
+constexpr int kBatchRows = 32;
 
 template <int OP>
 __global__ void __launch_bounds__(256) advect_batch_kernel(const AdvectJob* __restrict__ jobs,
@@ -152,14 +155,19 @@ __global__ void __launch_bounds__(256) advect_batch_kernel(const AdvectJob* __re
     const AdvectJob& J = jobs[g];
     const int lb = b - __ldg(prefix + g);
     const int bx = (J.A.cols + 31) / 32;
-    const int i = (lb / bx) * 8 + threadIdx.y, j = (lb % bx) * 32 + threadIdx.x;
+    const int j = (lb % bx) * 32 + threadIdx.x;
     int bad = 0;
-    if (OP == 0) {
-        if (i >= 1 && i < J.A.rows - 1 && j >= 1 && j < J.A.cols - 1) splat_cell(J.in0, J.in1, J.in2, J.out0, J.A, i, j);
-    } else if (OP == 1) {
-        if (i < J.A.rows && j < J.A.cols) bad = finish_cell(J.in0, J.out0, J.smooth, J.A, i, j);
-    } else {
-        if (i < J.A.rows && j < J.A.cols) advect_cell(J.in0, J.in1, J.out0, J.out1, J.A, i, j);
+#pragma unroll
+    for (int r = 0; r < kBatchRows; r += 8) {
+        const int i = (lb / bx) * kBatchRows + r + threadIdx.y;
+        if (OP == 0) {
+            if (i >= 1 && i < J.A.rows - 1 && j >= 1 && j < J.A.cols - 1)
+                splat_cell(J.in0, J.in1, J.in2, J.out0, J.A, i, j);
+        } else if (OP == 1) {
+            if (i < J.A.rows && j < J.A.cols) bad |= finish_cell(J.in0, J.out0, J.smooth, J.A, i, j);
+        } else {
+            if (i < J.A.rows && j < J.A.cols) advect_cell(J.in0, J.in1, J.out0, J.out1, J.A, i, j);
+        }
     }
     if (bad && nonfinite) atomicOr(nonfinite, 1);
 }
@@ -194,7 +202,7 @@ cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, f
     return cudaGetLastError();
 }
 
-int advect_batch_blocks(int rows, int cols) { return ((cols + 31) / 32) * ((rows + 7) / 8); }
+int advect_batch_blocks(int rows, int cols) { return ((cols + 31) / 32) * ((rows + kBatchRows - 1) / kBatchRows); }
 
 cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                 int* nonfinite, cudaStream_t st) {

@@ -182,8 +182,8 @@ cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, l
                                const int* converged, unsigned long long* counters, cudaStream_t st);
 
 int advect_batch_blocks(int rows, int cols);
-// op 0: splat, 1: density finish, 2: velocity backtrace; prefix[g] = first 32x8
-// block of job g, block_job[b] = job of block b.
+// op 0: splat, 1: density finish, 2: velocity backtrace; each block (32x8 threads)
+// covers 32x32 cells; prefix[g] = first block of job g, block_job[b] = job of block b.
 cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                 int* nonfinite, cudaStream_t st);
 // Stencil pass over a device table of fields (batched grids); prefix[f] = first tile
