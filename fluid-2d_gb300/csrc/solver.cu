@@ -134,6 +134,10 @@ struct fs_solver {
     int d_events_cap = 0;
     bool net_ready = false;
     cudaStream_t stream = nullptr;
+    // fs_solve_host on large grids: upload and download streams beside `stream`, and
+    // the events that order them (created by the first such call)
+    cudaStream_t xfer[2] = {};
+    cudaEvent_t xev[5] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool graph_valid = false;
@@ -668,6 +672,18 @@ int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const fl
     return FS_OK;
 }
 
+// Velocity half of a step from the diffused velocity: project into the state, advect by
+// itself, project again.
+int enqueue_velocity_tail(fs_solver* s, const float* dif_u, const float* dif_v, float dt, Counter& cnt) {
+    int rc;
+    if ((rc = enqueue_project(s, dif_u, dif_v, s->st[F_U], s->st[F_V], 0, cnt)) != FS_OK) return rc;
+    PROF_BEGIN(s);
+    CK(launch_advect_velocity(s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], advect_args(s, dt), s->stream));
+    PROF_END(s, FS_KIND_ADVECT, 16.0 * interior_cells(s));  // read u0, v0; write u, v
+    cnt.launches++;
+    return enqueue_project(s, s->vel1[0], s->vel1[1], s->st[F_U], s->st[F_V], 1, cnt);
+}
+
 int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
     int rc;
     if (s->cfg.method == FS_METHOD_GAUSS_SEIDEL) {
@@ -694,13 +710,7 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
     // density: forward advection by the step's initial velocity, then smoothing
     if ((rc = enqueue_advect_density(s, dif[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt)) != FS_OK) return rc;
     // velocity: project, advect by itself, project
-    if ((rc = enqueue_project(s, dif[F_U], dif[F_V], s->st[F_U], s->st[F_V], 0, cnt)) != FS_OK) return rc;
-    PROF_BEGIN(s);
-    CK(launch_advect_velocity(s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], advect_args(s, dt), s->stream));
-    PROF_END(s, FS_KIND_ADVECT, 16.0 * interior_cells(s));  // read u0, v0; write u, v
-    cnt.launches++;
-    if ((rc = enqueue_project(s, s->vel1[0], s->vel1[1], s->st[F_U], s->st[F_V], 1, cnt)) != FS_OK) return rc;
-    return FS_OK;
+    return enqueue_velocity_tail(s, dif[F_U], dif[F_V], dt, cnt);
 }
 
 void destroy_graph(fs_solver* s) {
@@ -802,15 +812,17 @@ int copy_in(fs_solver* s, float* dst, const float* host) {
     return FS_OK;
 }
 
-int copy_out(fs_solver* s, float* host, const float* src) {
+int copy_out(fs_solver* s, float* host, const float* src, cudaStream_t st) {
     CK(cudaMemcpy2DAsync(host, s->cols * sizeof(float), src, s->pitch * sizeof(float), s->cols * sizeof(float),
-                         s->rows, cudaMemcpyDeviceToHost, s->stream));
+                         s->rows, cudaMemcpyDeviceToHost, st));
     return FS_OK;
 }
+int copy_out(fs_solver* s, float* host, const float* src) { return copy_out(s, host, src, s->stream); }
 
-// Dense (rows x cols) staging buffers -> pitched fields, six at once: host uploads go
-// to contiguous scratch first because contiguous host-to-device copies run ~35 % faster
-// than row-by-row 2D copies into the pitched layout.
+// Dense (rows x cols) staging buffers -> pitched fields, up to six at once (one per
+// blockIdx.y): host uploads go to contiguous scratch first because contiguous
+// host-to-device copies run ~35 % faster than row-by-row 2D copies into the pitched
+// layout.
 struct Repack6 {
     const float* src[6];
     float* dst[6];
@@ -1090,6 +1102,13 @@ int fs_destroy(fs_solver* s) {
     if (!s) return FS_OK;
     DeviceGuard g(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (cudaStream_t x : s->xfer)
+        if (x) {
+            cudaStreamSynchronize(x);
+            cudaStreamDestroy(x);
+        }
+    for (cudaEvent_t e : s->xev)
+        if (e) cudaEventDestroy(e);
     destroy_graph(s);
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->net.mem) cudaFree(s->net.mem);
@@ -1142,12 +1161,96 @@ int fs_sync(fs_solver* s) {
     return check_flags(s);
 }
 
+// Grids of at least this many cells take the overlapped host step below. On smaller
+// grids the copies are shorter than what the overlap costs (an eager step in place of one
+// graph launch, and the diffusion split into two launches).
+#ifndef FS_OVERLAP_MIN_CELLS
+#define FS_OVERLAP_MIN_CELLS (1L << 20)
+#endif
+
+namespace {
+
+int launch_repack(fs_solver* s, float* const* stage, float* const* dst, int count) {
+    Repack6 R{};
+    for (int k = 0; k < count; ++k) {
+        R.src[k] = stage[k];
+        R.dst[k] = dst[k];
+    }
+    repack_kernel<<<dim3(152 * 2, count), 256, 0, s->stream>>>(R, s->rows, s->cols, s->pitch);
+    CK(cudaGetLastError());
+    return FS_OK;
+}
+
+// One Jacobi step on host grids with the copies overlapped: density and its source go up
+// first and density diffuses while the four velocity grids are still on their way; the
+// new density goes down while the velocity is projected and advected. Each field sees
+// the same kernels as in enqueue_step, so the results are those of upload + step +
+// download. host: density, u, v, density source, u source, v source; out: density, u, v.
+int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const out[3], float diff, float visc,
+                          float dt) {
+    if (!s->xfer[0]) {
+        for (cudaStream_t& x : s->xfer) CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : s->xev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaStream_t up = s->xfer[0], down = s->xfer[1];
+    const size_t bytes = (size_t)s->rows * s->cols * sizeof(float);
+    // staging: scratch that the step overwrites after reading it (diffusion x0 and the
+    // first ping-pong buffer of each field)
+    float* stage[6] = {s->x0[F_D], s->pp[F_D][0], s->x0[F_U], s->x0[F_V], s->pp[F_U][0], s->pp[F_V][0]};
+    const float* from[6] = {host[0], host[3], host[1], host[2], host[4], host[5]};
+    float* dst[6] = {s->st[F_D], s->src[F_D], s->st[F_U], s->st[F_V], s->src[F_U], s->src[F_V]};
+    // uploads begin after the handle's earlier work, which may still read the scratch
+    CK(cudaEventRecord(s->xev[0], s->stream));
+    CK(cudaStreamWaitEvent(up, s->xev[0], 0));
+    for (int k = 0; k < 2; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
+    CK(cudaEventRecord(s->xev[1], up));
+    Counter cnt;
+    int rc;
+    CK(cudaStreamWaitEvent(s->stream, s->xev[1], 0));
+    if ((rc = launch_repack(s, stage, dst, 2)) != FS_OK) return rc;
+    const int fd = F_D, fuv[2] = {F_U, F_V};
+    const float rd = diff, ruv[2] = {visc, visc};
+    float *dif_d, *dif_uv[2];
+    if ((rc = enqueue_diffuse(s, &fd, 1, &rd, dt, &dif_d, cnt)) != FS_OK) return rc;
+    // issued after the density work so that a pageable (host-blocking) copy still overlaps it
+    for (int k = 2; k < 6; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
+    CK(cudaEventRecord(s->xev[2], up));
+    CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
+    if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
+    if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
+    if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt)) != FS_OK) return rc;
+    CK(cudaEventRecord(s->xev[3], s->stream));
+    if ((rc = enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt)) != FS_OK) return rc;
+    // the density download is issued after the velocity work for the same reason
+    CK(cudaStreamWaitEvent(down, s->xev[3], 0));
+    if ((rc = copy_out(s, out[0], s->st[F_D], down)) != FS_OK) return rc;
+    CK(cudaEventRecord(s->xev[4], down));
+    if ((rc = copy_out(s, out[1], s->st[F_U])) || (rc = copy_out(s, out[2], s->st[F_V]))) return rc;
+    CK(cudaStreamWaitEvent(s->stream, s->xev[4], 0));
+    cnt.launches += 2;
+    s->launches_per_step = cnt.launches;
+    s->passes_per_step = cnt.passes;
+    s->stats.kernel_launches += cnt.launches;
+    s->warm_valid = true;
+    s->stats.steps++;
+    return FS_OK;
+}
+
+}  // namespace
+
 int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate, float* u,
                   float* v, const float* u_source, const float* v_source, float viscosity, float dt) {
     if (!s || !density || !density_source || !u || !v || !u_source || !v_source)
         return fail(FS_ERR_ARG, "fs_solve_host: null argument");
     DeviceGuard g(s->device);
     int rc;
+    if (s->cfg.method == FS_METHOD_JACOBI && (long)s->rows * s->cols >= FS_OVERLAP_MIN_CELLS) {
+        const float* host[6] = {density, u, v, density_source, u_source, v_source};
+        float* const out[3] = {density, u, v};
+        if ((rc = solve_host_overlapped(s, host, out, diffusion_rate, viscosity, dt)) != FS_OK) return rc;
+        CK(cudaStreamSynchronize(s->stream));
+        return check_flags(s);
+    }
     // stage the six inputs densely in scratch fields the step overwrites anyway, then
     // spread them into the pitched state and source fields with one kernel
     const float* host[6] = {density, u, v, density_source, u_source, v_source};

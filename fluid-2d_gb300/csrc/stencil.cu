@@ -15,9 +15,11 @@
 //
 // Each thread owns one column of SR consecutive rows and keeps its constant terms
 // (x0 or div) in registers; every sweep streams down the column from the shared copy
-// of the previous sweep (double-buffered, one barrier per sweep, a second one only in
-// CTAs whose region touches a domain edge) as two rolling windows in lockstep, so
-// each pair of cell updates issues as packed f32x2 instructions. All arithmetic uses
+// of the previous sweep (double-buffered, one barrier per sweep) as two rolling
+// windows in lockstep, so each pair of cell updates issues as packed f32x2
+// instructions. The reference's per-sweep boundary fill is folded into the sweep (the
+// cells next to a domain edge read what the fill would have stored there) and applied
+// for real once, after the last sweep. All arithmetic uses
 // explicit round-to-nearest intrinsics in the reference's operand order, so no FMA
 // contraction changes its rounding (the one multiply feeding an add stays scalar). The reference divides by (1.0 + 4.0*a) in
 // double; FP64 is slow on GB300, so the quotient is formed as
@@ -90,14 +92,23 @@ __device__ __forceinline__ float2 pressure_update2(float2 dv, float2 L, float2 R
 //   EDGE = false: the region lies inside the domain interior; every cell updates, no
 //                 checks (cells near the region border compute values that nothing
 //                 stored depends on).
-//   EDGE = true:  bit i of `live` marks interior cells (others keep their value); after
-//                 each sweep the domain-edge cells take their inner neighbour's new value
-//                 (set_boundary_*, fluid_solver_gpu.cu:11-54); corners keep theirs.
+//   EDGE = true:  bit i of `live` marks interior cells (others keep their value). The
+//                 reference fills the domain-edge cells after every sweep with their
+//                 inner neighbour's new value times a sign (set_boundary_*,
+//                 fluid_solver_gpu.cu:11-54), and the only cells that read an edge cell
+//                 are those inner neighbours. So from the second sweep on, an interior
+//                 cell next to an edge reads sign * (its own current value) in place of
+//                 the edge cell — the same float the fill would have stored there — and
+//                 the edge cells themselves are filled once, after the last sweep, by
+//                 fill_edges. The first sweep reads the edge cells as loaded.
+//                 up_bits / dn_bits: bit i set where row r0 + i is grid row 1 / rows - 2
+//                 (its upper / lower neighbour is an edge cell); at_left / at_right: this
+//                 column is grid column 1 / cols - 2.
 template <bool DIFF, bool EDGE, int SR, int RH>
 __device__ __forceinline__ void run_sweeps(const float2 (&k2)[SR / 2], int& co, int& no, int nsweeps, int r0,
-                                           int tx, int txl, int txr, unsigned live, int gy0, int gc, int rows,
-                                           int cols, float s_lr, float s_tb, float a, float dh, float dl,
-                                           float rf) {
+                                           int tx, int txl, int txr, unsigned live, unsigned up_bits,
+                                           unsigned dn_bits, bool at_left, bool at_right, float s_lr, float s_tb,
+                                           float a, float dh, float dl, float rf) {
     constexpr int RW = kRegionW, H2 = SR / 2;
     extern __shared__ float4 smem4[];
     float* const S = reinterpret_cast<float*>(smem4);
@@ -116,16 +127,28 @@ __device__ __forceinline__ void run_sweeps(const float2 (&k2)[SR / 2], int& co, 
         const float* __restrict__ cl = c + l_off;
         const float* __restrict__ cr = c + r_off;
         float* __restrict__ nx = S + no + base;
+        // edge folding starts with the second sweep
+        const unsigned ub = s > 0 ? up_bits : 0u, db = s > 0 ? dn_bits : 0u;
+        const bool fl = s > 0 && at_left, fr = s > 0 && at_right;
         // two rolling windows down the segment in lockstep: rows j (x) and j + SR/2 (y)
         float2 up = make_float2(c[up_off], c[(H2 - 1) * RW]);
         float2 ce = make_float2(c[0], c[H2 * RW]);
 #pragma unroll
         for (int j = 0; j < H2; ++j) {
             const float2 dn = make_float2(c[(j + 1) * RW], j + 1 + H2 < SR ? c[(j + 1 + H2) * RW] : c[dn_off]);
-            const float2 Lv = make_float2(cl[j * RW], cl[(j + H2) * RW]);
-            const float2 Rv = make_float2(cr[j * RW], cr[(j + H2) * RW]);
-            float2 nv = DIFF ? diffuse_update2(k2[j], Lv, Rv, up, dn, a2, ndh2, ndl2, rf2)
-                             : pressure_update2(k2[j], Lv, Rv, up, dn);
+            float2 Lv = make_float2(cl[j * RW], cl[(j + H2) * RW]);
+            float2 Rv = make_float2(cr[j * RW], cr[(j + H2) * RW]);
+            float2 Dv = dn;
+            if (EDGE) {
+                if ((ub >> j) & 1u) up.x = __fmul_rn(s_tb, ce.x);
+                if ((ub >> (j + H2)) & 1u) up.y = __fmul_rn(s_tb, ce.y);
+                if ((db >> j) & 1u) Dv.x = __fmul_rn(s_tb, ce.x);
+                if ((db >> (j + H2)) & 1u) Dv.y = __fmul_rn(s_tb, ce.y);
+                if (fl) Lv = make_float2(__fmul_rn(s_lr, ce.x), __fmul_rn(s_lr, ce.y));
+                if (fr) Rv = make_float2(__fmul_rn(s_lr, ce.x), __fmul_rn(s_lr, ce.y));
+            }
+            float2 nv = DIFF ? diffuse_update2(k2[j], Lv, Rv, up, Dv, a2, ndh2, ndl2, rf2)
+                             : pressure_update2(k2[j], Lv, Rv, up, Dv);
             if (EDGE) {
                 nv.x = ((live >> j) & 1u) ? nv.x : ce.x;
                 nv.y = ((live >> (j + H2)) & 1u) ? nv.y : ce.y;
@@ -136,29 +159,40 @@ __device__ __forceinline__ void run_sweeps(const float2 (&k2)[SR / 2], int& co, 
             ce = dn;
         }
         __syncthreads();
-        if (EDGE) {
-            const bool col_int = gc >= 1 && gc <= cols - 2;
-            for (int i = 0; i < SR; ++i) {
-                const int r = r0 + i, gr = gy0 + r;
-                int src = -1;
-                float sg = 1.f;
-                if (col_int) {
-                    if (gr == 0) src = min(r + 1, RH - 1) * RW + tx;
-                    else if (gr == rows - 1) src = max(r - 1, 0) * RW + tx;
-                    sg = s_tb;
-                } else if (gr >= 1 && gr <= rows - 2) {
-                    if (gc == 0) src = r * RW + txr;
-                    else if (gc == cols - 1) src = r * RW + txl;
-                    sg = s_lr;
-                }
-                if (src >= 0) S[no + r * RW + tx] = sg * S[no + src];
-            }
-            __syncthreads();
-        }
         const int t = co;
         co = no;
         no = t;
     }
+}
+
+// The reference's boundary fill applied once to the final sweep in S + co: edge cells
+// (corners excepted) take their inner neighbour's value times the field's sign. Reads
+// touch interior cells only and writes edge cells only, so one barrier after suffices.
+template <int SR, int RH>
+__device__ __forceinline__ void fill_edges(int co, int r0, int tx, int txl, int txr, int g0, int gc, int rows,
+                                           int cols, float s_lr, float s_tb) {
+    constexpr int RW = kRegionW;
+    extern __shared__ float4 smem4[];
+    float* const S = reinterpret_cast<float*>(smem4) + co;
+    if (gc >= 1 && gc <= cols - 2) {
+        const int it = -g0, ib = rows - 1 - g0;  // segment rows of grid rows 0 and rows - 1
+        if (it >= 0 && it < SR) {
+            const int r = r0 + it;
+            S[r * RW + tx] = s_tb * S[min(r + 1, RH - 1) * RW + tx];
+        }
+        if (ib >= 0 && ib < SR) {
+            const int r = r0 + ib;
+            S[r * RW + tx] = s_tb * S[max(r - 1, 0) * RW + tx];
+        }
+    } else if (gc == 0 || gc == cols - 1) {
+        const int src = gc == 0 ? txr : txl;
+#pragma unroll
+        for (int i = 0; i < SR; ++i) {
+            const int gr = g0 + i;
+            if (gr >= 1 && gr <= rows - 2) S[(r0 + i) * RW + tx] = s_lr * S[(r0 + i) * RW + src];
+        }
+    }
+    __syncthreads();
 }
 
 // One tile of one pass: load the region (fusing add_sources or the divergence into
@@ -260,10 +294,14 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // ------------------------------------------------------------------ sweeps
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
     if (edge_cta) {
-        run_sweeps<DIFF, true, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, m_int, gy0, gc, rows, cols, F.s_lr,
-                                       F.s_tb, F.a, F.dh, F.dl, F.rf);
+        const int i1 = 1 - g0, i2 = rows - 2 - g0;  // segment rows of grid rows 1 and rows - 2
+        const unsigned up_bits = (i1 >= 0 && i1 < SR) ? 1u << i1 : 0u;
+        const unsigned dn_bits = (i2 >= 0 && i2 < SR) ? 1u << i2 : 0u;
+        run_sweeps<DIFF, true, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, m_int, up_bits, dn_bits, gc == 1,
+                                       gc == cols - 2, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf);
+        if (F.sweeps > 0) fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
     } else {
-        run_sweeps<DIFF, false, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, 0u, gy0, gc, rows, cols, F.s_lr,
+        run_sweeps<DIFF, false, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, 0u, 0u, 0u, false, false, F.s_lr,
                                         F.s_tb, F.a, F.dh, F.dl, F.rf);
     }
     // final values of this thread's column (S + co is complete after the last barrier)
