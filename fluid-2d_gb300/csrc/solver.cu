@@ -134,6 +134,10 @@ struct fs_solver {
     int d_events_cap = 0;
     bool net_ready = false;
     cudaStream_t stream = nullptr;
+    // density advection runs on `side` beside the first projection (a parallel branch of
+    // the step graph), forked and joined by side_ev
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_ev[2] = {};
     // fs_solve_host on large grids: upload and download streams beside `stream`, and
     // the events that order them (created by the first such call)
     cudaStream_t xfer[2] = {};
@@ -179,6 +183,17 @@ int default_sweeps(const fs_config* cfg, int dev, int maxk) {
     const int total = std::max(cfg->diffuse_iterations, cfg->pressure_iterations);
     const int passes = std::max(1, (total + kmax - 1) / kmax);
     return std::max(k8, (total + passes - 1) / passes);
+}
+
+// The step's stream at the device's highest priority and the side stream (density
+// advection) at its lowest, so that the side branch of a step takes only the SMs the
+// pressure passes leave free.
+cudaError_t create_streams(fs_solver* s) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
+    return cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, least);
 }
 
 // Split `total` sweeps into passes of at most `k` (at least one pass, possibly of
@@ -681,31 +696,57 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
 }
 
 int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const float* u, const float* v, float dt,
-                           Counter& cnt) {
+                           Counter& cnt, cudaStream_t st) {
     const AdvectArgs A = advect_args(s, dt);
     PROF_BEGIN(s);
-    CK(cudaMemsetAsync(s->acc, 0, s->field_floats * sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->acc, 0, s->field_floats * sizeof(float), st));
     PROF_END(s, FS_KIND_MEMSET, 0.0);
     PROF_BEGIN(s);
-    CK(launch_splat(d0, u, v, s->acc, A, s->stream));
+    CK(launch_splat(d0, u, v, s->acc, A, st));
     PROF_END(s, FS_KIND_SPLAT, 16.0 * interior_cells(s));  // read d0, u, v; write d
     PROF_BEGIN(s);
-    CK(launch_density_finish(s->acc, d_out, s->cfg.smooth, A, s->cfg.check_finite ? s->flags : nullptr,
-                             s->stream));
+    CK(launch_density_finish(s->acc, d_out, s->cfg.smooth, A, s->cfg.check_finite ? s->flags : nullptr, st));
     PROF_END(s, FS_KIND_FINISH, 8.0 * interior_cells(s));  // smooth: read d, write d
     cnt.launches += 2;
     return FS_OK;
 }
 
-// Velocity half of a step from the diffused velocity: project into the state, advect by
-// itself, project again.
+// The density half of a step after diffusion: forward advection of the diffused density
+// by the step's initial velocity (still in the state), then smoothing. It depends on
+// nothing the velocity half writes before its second projection, so outside profiled
+// steps it runs on the side stream, beside the first projection and the velocity
+// advection, and join_density() brings it back before the state velocity is rewritten.
+int fork_density(fs_solver* s, const float* dif_d, float dt, Counter& cnt) {
+    cudaStream_t st = s->stream;
+    if (!s->prof) {
+        CK(cudaEventRecord(s->side_ev[0], s->stream));
+        CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
+        st = s->side;
+    }
+    int rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, st);
+    if (rc != FS_OK) return rc;
+    if (!s->prof) CK(cudaEventRecord(s->side_ev[1], s->side));
+    return FS_OK;
+}
+
+int join_density(fs_solver* s) {
+    if (!s->prof) CK(cudaStreamWaitEvent(s->stream, s->side_ev[1], 0));
+    return FS_OK;
+}
+
+// Velocity half of a step from the diffused velocity: project (into the u/v diffusion
+// scratch, free by now, so that the state keeps the initial velocity the density
+// advection reads), advect by itself, join the density half, project into the state.
 int enqueue_velocity_tail(fs_solver* s, const float* dif_u, const float* dif_v, float dt, Counter& cnt) {
     int rc;
-    if ((rc = enqueue_project(s, dif_u, dif_v, s->st[F_U], s->st[F_V], 0, cnt)) != FS_OK) return rc;
+    float* pu = s->x0[F_U];
+    float* pv = s->x0[F_V];
+    if ((rc = enqueue_project(s, dif_u, dif_v, pu, pv, 0, cnt)) != FS_OK) return rc;
     PROF_BEGIN(s);
-    CK(launch_advect_velocity(s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], advect_args(s, dt), s->stream));
+    CK(launch_advect_velocity(pu, pv, s->vel1[0], s->vel1[1], advect_args(s, dt), s->stream));
     PROF_END(s, FS_KIND_ADVECT, 16.0 * interior_cells(s));  // read u0, v0; write u, v
     cnt.launches++;
+    if ((rc = join_density(s)) != FS_OK) return rc;
     return enqueue_project(s, s->vel1[0], s->vel1[1], s->st[F_U], s->st[F_V], 1, cnt);
 }
 
@@ -732,9 +773,9 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
     const float rates[3] = {diff, visc, visc};
     float* dif[3];
     if ((rc = enqueue_diffuse(s, fields, 3, rates, dt, dif, cnt)) != FS_OK) return rc;
-    // density: forward advection by the step's initial velocity, then smoothing
-    if ((rc = enqueue_advect_density(s, dif[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt)) != FS_OK) return rc;
-    // velocity: project, advect by itself, project
+    // density: forward advection by the step's initial velocity, then smoothing (beside
+    // the velocity half); velocity: project, advect by itself, project
+    if ((rc = fork_density(s, dif[F_D], dt, cnt)) != FS_OK) return rc;
     return enqueue_velocity_tail(s, dif[F_U], dif[F_V], dt, cnt);
 }
 
@@ -762,7 +803,7 @@ int run_steps(fs_solver* s, float diff, float visc, float dt, int nsteps) {
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(s->stream, &g);
             cudaGraphExec_t ge = nullptr;
-            if (rc == FS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+            if (rc == FS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, cudaGraphInstantiateFlagUseNodePriority);
             if (rc != FS_OK || e != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
                 if (s->cfg.pressure_tolerance > 0.f) {
@@ -1054,7 +1095,9 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     int rc = FS_OK;
     if ((e = cudaMemset(s->slab, 0, slab_bytes)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaMemset");
-    else if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    else if ((e = create_streams(s)) != cudaSuccess ||
+             (e = cudaEventCreateWithFlags(&s->side_ev[0], cudaEventDisableTiming)) != cudaSuccess ||
+             (e = cudaEventCreateWithFlags(&s->side_ev[1], cudaEventDisableTiming)) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: cudaStreamCreate");
     if (rc == FS_OK && learned) {
         // coarse grid: learned_grid, else 32 (a finer 64 grid resolves more modes, but the
@@ -1133,6 +1176,12 @@ int fs_destroy(fs_solver* s) {
             cudaStreamDestroy(x);
         }
     for (cudaEvent_t e : s->xev)
+        if (e) cudaEventDestroy(e);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    for (cudaEvent_t e : s->side_ev)
         if (e) cudaEventDestroy(e);
     destroy_graph(s);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -1243,8 +1292,8 @@ int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const
     CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
     if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
     if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
-    if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt)) != FS_OK) return rc;
-    CK(cudaEventRecord(s->xev[3], s->stream));
+    if ((rc = fork_density(s, dif_d, dt, cnt)) != FS_OK) return rc;
+    CK(cudaEventRecord(s->xev[3], s->side));
     if ((rc = enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt)) != FS_OK) return rc;
     // the density download is issued after the velocity work for the same reason
     CK(cudaStreamWaitEvent(down, s->xev[3], 0));
@@ -1390,7 +1439,7 @@ int fs_stage(fs_solver* s, int stage, float rate, float dt) {
             break;
         }
         case FS_STAGE_ADVECT_DENSITY:
-            rc = enqueue_advect_density(s, s->st[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt);
+            rc = enqueue_advect_density(s, s->st[F_D], s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, s->stream);
             break;
         case FS_STAGE_PROJECT:
             if ((rc = enqueue_project(s, s->st[F_U], s->st[F_V], s->vel1[0], s->vel1[1], 0, cnt)) == FS_OK &&
