@@ -195,6 +195,30 @@ __device__ __forceinline__ void fill_edges(int co, int r0, int tx, int txl, int 
     __syncthreads();
 }
 
+// Tile b of a pass in dispatch order: the domain-edge tiles first (their sweeps carry
+// the edge folding and a final fill, ~20 % more time), then the interior row by row, so
+// that the last tiles a pass starts are the short ones.
+__device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi, int& txi) {
+    if (tx_n <= 2 || ty_n <= 2) {
+        tyi = b / tx_n;
+        txi = b - tyi * tx_n;
+        return;
+    }
+    const int side = ty_n - 2;
+    if (b < 2 * tx_n) {  // top and bottom rows
+        tyi = b < tx_n ? 0 : ty_n - 1;
+        txi = b < tx_n ? b : b - tx_n;
+    } else if (b < 2 * tx_n + 2 * side) {  // left and right columns
+        const int k = b - 2 * tx_n;
+        tyi = 1 + (k < side ? k : k - side);
+        txi = k < side ? 0 : tx_n - 1;
+    } else {
+        const int k = b - 2 * tx_n - 2 * side, w = tx_n - 2;
+        tyi = 1 + k / w;
+        txi = 1 + (k - (k / w) * w);
+    }
+}
+
 // One tile of one pass: load the region (fusing add_sources or the divergence into
 // the first pass), run F.sweeps sweeps with the boundary fill after each, store the
 // output tile, then the optional gradient-subtract epilogue and the optional residual
@@ -209,7 +233,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     float* const S = reinterpret_cast<float*>(smem4);
     int co = 0, no = RH * RW;  // offsets of the current / next sweep buffers in S
     __syncthreads();  // the previous tile of this CTA may still be reading shared memory
-    const int tyi = b / F.tiles_x, txi = b - tyi * F.tiles_x;
+    int tyi, txi;
+    tile_coords(b, F.tiles_x, F.tiles_y, tyi, txi);
     const int H = F.halo;
     const int gy0 = tyi * F.tile_h - F.shift_y - H;
     const int gx0 = txi * F.tile_w - F.shift_x - H;
