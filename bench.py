@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--cycle-iters", type=int, default=128, help="learned: Jacobi sweeps after each correction")
     ap.add_argument("--train-size", type=int, default=512, help="learned: grid of the training runs")
     ap.add_argument("--learned-grid", type=int, default=0, help="learned: coarse grid side (0 = default, 32, 64)")
+    ap.add_argument("--modes", default="previous,learned,coarse_only",
+                    help="learned: pressure starts to compare (zero, previous, learned, coarse_only)")
     ap.add_argument("--mid-solve-samples", type=int, default=0,
                     help="learned: add this many mid-solve states met by a first-round network, then retrain")
     return ap.parse_args()
@@ -724,8 +726,10 @@ def run_learned(a):
         w = workloads.vortex_field(size, seed=3, kd=a.kd, kp=a.kp)
         for tol in [float(x) for x in a.tols.split(",")]:
             row = {"size": size, "tol": tol}
-            modes = (("previous", pkg.FS_WARM_PREVIOUS, None), ("learned", pkg.FS_WARM_LEARNED, params),
-                     ("coarse_only", pkg.FS_WARM_LEARNED, np.zeros_like(params)))
+            all_modes = {"zero": (pkg.FS_WARM_ZERO, None), "previous": (pkg.FS_WARM_PREVIOUS, None),
+                         "learned": (pkg.FS_WARM_LEARNED, params),
+                         "coarse_only": (pkg.FS_WARM_LEARNED, np.zeros_like(params))}
+            modes = [(m,) + all_modes[m] for m in a.modes.split(",")]
             for mode, warm, net_params in modes:
                 s = pkg.Solver(w.rows, w.cols, diffuse_iterations=a.kd, pressure_tolerance=tol,
                                pressure_max_iterations=a.max_iters, warm_start=warm, device=0, check_finite=0,
@@ -760,8 +764,11 @@ def run_learned(a):
                     used, fb = st["learned_used"], st["learned_fallback"]
                     row[mode]["fallback_rate"] = fb / max(1, used + fb)
                 s.close()
-            row["speedup_ms"] = row["previous"]["ms_per_step"] / row["learned"]["ms_per_step"]
-            row["speedup_vs_coarse_only"] = row["coarse_only"]["ms_per_step"] / row["learned"]["ms_per_step"]
+            if "learned" in row:
+                for base in ("zero", "previous", "coarse_only"):
+                    if base in row:
+                        key = "speedup_ms" if base == "previous" else f"speedup_vs_{base}"
+                        row[key] = row[base]["ms_per_step"] / row["learned"]["ms_per_step"]
             results.append(row)
             print(json.dumps(row), flush=True)
     line = {"metric": "ms/step to relative pressure residual, learned vs previous-pressure warm start",
