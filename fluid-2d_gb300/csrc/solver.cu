@@ -148,6 +148,8 @@ struct fs_solver {
     float g_diff = 0, g_visc = 0, g_dt = 0;
     int sweeps = 8;
     int tile_rows = 64;
+    // diffuse the density on the side branch too (see density_branch_pays)
+    bool density_branch = false;
     int launches_per_step = 0;
     int passes_per_step = 0;
     bool warm_valid = false;
@@ -194,6 +196,22 @@ cudaError_t create_streams(fs_solver* s) {
     if (e != cudaSuccess) return e;
     if ((e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
     return cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, least);
+}
+
+// Whether to diffuse the density on the step's side branch instead of in the same
+// launches as u and v. Fields are independent, so the density passes can fill the SMs the
+// u/v passes leave idle in their last wave; that pays where a fused three-field pass has
+// a short last wave among few (1024^2: 0.359 -> 0.335 ms per 40/40 step, 2048^2: 1.034 ->
+// 1.023 ms) and costs where the last wave is negligible (4096^2, 31 waves: +0.5 %) or the
+// step is launch-bound (130^2: +5 %). So: when the fused pass fills 1 to 12 waves.
+bool density_branch_pays(const fs_solver* s, int dev) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return false;
+    const int slots = sms * (s->tile_rows <= 64 ? 2 : 1);
+    const long tw = kRegionW - 2 * s->sweeps, th = s->tile_rows - 2 * s->sweeps;
+    if (tw <= 0 || th <= 0) return false;
+    const long tiles3 = 3 * ((s->cols + tw - 1) / tw) * ((s->rows + th - 1) / th);
+    return tiles3 >= slots && tiles3 <= 12L * slots;
 }
 
 // Split `total` sweeps into passes of at most `k` (at least one pass, possibly of
@@ -285,7 +303,8 @@ int prof_end(fs_solver* s, int kind, double bytes) {
 // Diffusion of a subset of {d, u, v}: add_sources fused into pass 0. Returns the
 // buffer holding each field's result in out[].
 int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates, float dt, float** out,
-                    Counter& cnt) {
+                    Counter& cnt, cudaStream_t st = nullptr) {
+    if (!st) st = s->stream;
     const std::vector<int> plan = split_sweeps(s->cfg.diffuse_iterations, s->sweeps);
     const float* cur[3] = {};
     for (int q = 0; q < nf; ++q) cur[q] = s->st[fields[q]];
@@ -321,7 +340,7 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
         // per field: 12 B/cell per sweep (read x and x0, write x) + 12 B/cell add_sources
         const double bytes = nf * interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0));
         PROF_BEGIN(s);
-        CK(launch_stencil(L, s->tile_rows, s->stream));
+        CK(launch_stencil(L, s->tile_rows, st));
         PROF_END(s, FS_KIND_STENCIL, bytes);
         cnt.launches++;
         cnt.passes++;
@@ -711,20 +730,27 @@ int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const fl
     return FS_OK;
 }
 
-// The density half of a step after diffusion: forward advection of the diffused density
-// by the step's initial velocity (still in the state), then smoothing. It depends on
-// nothing the velocity half writes before its second projection, so outside profiled
-// steps it runs on the side stream, beside the first projection and the velocity
-// advection, and join_density() brings it back before the state velocity is rewritten.
-int fork_density(fs_solver* s, const float* dif_d, float dt, Counter& cnt) {
+// The density half of a step: forward advection of the diffused density by the step's
+// initial velocity (still in the state), then smoothing — and, with diffuse = true, the
+// density diffusion before it. It depends on nothing the velocity half writes before its
+// second projection, so outside profiled steps it runs on the side stream, beside the
+// velocity diffusion and the first projection, and join_density() brings it back before
+// the state velocity is rewritten. dif_d: the diffused density when diffuse = false.
+int fork_density(fs_solver* s, const float* dif_d, float diff, float dt, bool diffuse, Counter& cnt) {
     cudaStream_t st = s->stream;
     if (!s->prof) {
         CK(cudaEventRecord(s->side_ev[0], s->stream));
         CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
         st = s->side;
     }
-    int rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, st);
-    if (rc != FS_OK) return rc;
+    int rc;
+    if (diffuse) {
+        const int fd = F_D;
+        float* out = nullptr;
+        if ((rc = enqueue_diffuse(s, &fd, 1, &diff, dt, &out, cnt, st)) != FS_OK) return rc;
+        dif_d = out;
+    }
+    if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, st)) != FS_OK) return rc;
     if (!s->prof) CK(cudaEventRecord(s->side_ev[1], s->side));
     return FS_OK;
 }
@@ -768,15 +794,25 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
         cnt.launches += 4;
         return FS_OK;
     }
-    // density and velocity diffusion are independent; one launch per pass serves all three
-    const int fields[3] = {F_D, F_U, F_V};
-    const float rates[3] = {diff, visc, visc};
-    float* dif[3];
-    if ((rc = enqueue_diffuse(s, fields, 3, rates, dt, dif, cnt)) != FS_OK) return rc;
-    // density: forward advection by the step's initial velocity, then smoothing (beside
-    // the velocity half); velocity: project, advect by itself, project
-    if ((rc = fork_density(s, dif[F_D], dt, cnt)) != FS_OK) return rc;
-    return enqueue_velocity_tail(s, dif[F_U], dif[F_V], dt, cnt);
+    if (s->prof || !s->density_branch) {
+        // one diffusion launch per pass serves all three fields (and profiled steps run
+        // sequentially)
+        const int fields[3] = {F_D, F_U, F_V};
+        const float rates[3] = {diff, visc, visc};
+        float* dif[3];
+        if ((rc = enqueue_diffuse(s, fields, 3, rates, dt, dif, cnt)) != FS_OK) return rc;
+        if ((rc = fork_density(s, dif[F_D], diff, dt, false, cnt)) != FS_OK) return rc;
+        return enqueue_velocity_tail(s, dif[F_U], dif[F_V], dt, cnt);
+    }
+    // density (diffusion, then forward advection by the step's initial velocity and
+    // smoothing) on the low-priority side branch; velocity: diffuse u and v in one launch
+    // per pass, project, advect by itself, project
+    if ((rc = fork_density(s, nullptr, diff, dt, true, cnt)) != FS_OK) return rc;
+    const int fuv[2] = {F_U, F_V};
+    const float ruv[2] = {visc, visc};
+    float* dif_uv[2];
+    if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
+    return enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt);
 }
 
 void destroy_graph(fs_solver* s) {
@@ -1036,6 +1072,7 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     s->tile_rows = cfg->tile_rows ? cfg->tile_rows : 64;
     const int maxk = stencil_max_halo(s->tile_rows) - 1;
     s->sweeps = cfg->sweeps_per_pass > 0 ? std::min(cfg->sweeps_per_pass, maxk) : default_sweeps(cfg, dev, maxk);
+    s->density_branch = density_branch_pays(s, dev);
 
     if (cfg->method == FS_METHOD_GAUSS_SEIDEL && cfg->rows > gs_max_size()) {
         delete s;
@@ -1292,7 +1329,7 @@ int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const
     CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
     if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
     if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
-    if ((rc = fork_density(s, dif_d, dt, cnt)) != FS_OK) return rc;
+    if ((rc = fork_density(s, dif_d, diff, dt, false, cnt)) != FS_OK) return rc;
     CK(cudaEventRecord(s->xev[3], s->side));
     if ((rc = enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt)) != FS_OK) return rc;
     // the density download is issued after the velocity work for the same reason
