@@ -8,8 +8,8 @@
 // That is ~20 B/cell of HBM traffic and two launches per sweep. Here one launch runs
 // `sweeps` sweeps of one or more fields: each CTA loads a 128-column region (its
 // output tile grown by a halo H >= sweeps), iterates in shared memory with the
-// boundary fill applied after every sweep exactly as the reference does, and writes
-// only its output tile back. The first pass of a solve fuses what precedes it
+// boundary fill's effect reproduced exactly after every sweep, and writes only its
+// output tile back. The first pass of a solve fuses what precedes it
 // (add_sources for diffusion, the divergence for pressure) and the last pressure
 // pass fuses the gradient subtract and the two reflecting fills.
 //
@@ -220,7 +220,8 @@ __device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi,
 }
 
 // One tile of one pass: load the region (fusing add_sources or the divergence into
-// the first pass), run F.sweeps sweeps with the boundary fill after each, store the
+// the first pass), run F.sweeps sweeps (edge CTAs: with the boundary fill folded in and
+// applied once at the end), store the
 // output tile, then the optional gradient-subtract epilogue and the optional residual
 // partial sums (for residual-driven pressure solves). xin/yout stand in for F.x/F.y so
 // a persistent caller can ping-pong buffers across passes.
