@@ -13,7 +13,10 @@ seeded low-frequency noise, no sources. Metric: interior cell-steps per second.
             reference's fluid_solver_gpu::solve.
   roofline  stencil kernels (the dominant kind): algorithmic bytes per launch (the
             per-sweep model 12 B/cell/sweep + fused work) over their CUDA-event time
-            in profiled steps, against the measured HBM copy bandwidth.
+            in profiled steps, against the measured HBM copy bandwidth. A profiled step
+            runs its kernels one after another with events between them, so its
+            diffusion passes are the fused three-field launches, where the timed step
+            graph may run the density's passes on a side branch.
   cpu_baseline  the oracle's Jacobi restatement of the same step (OpenMP, all host
             cores) on a bounded sample.
 

@@ -25,3 +25,17 @@ def test_autotune_picks_caches_and_keeps_parity(fluid, wl, tmp_path):
                             kd=20, kp=20, nsteps=3)
     for g, o in zip((d, u, v), want):
         assert oracle.rel_linf(g, o) <= 1e-5
+
+
+def test_default_depth_rule(fluid):
+    """sweeps_per_pass = 0: depth 8 on large grids and residual-target solves; the fewest
+    passes on launch-bound small grids; an explicit depth is kept."""
+    def depth(n, **kw):
+        with fluid.Solver(n, n, device=0, **kw) as s:
+            return s.stats()["sweeps_per_pass"]
+
+    assert depth(130) == 20                                  # 15/20 sweeps: one pass per solve
+    assert depth(130, diffuse_iterations=40, pressure_iterations=40) == 20  # two passes of 20
+    assert depth(2050) == 8
+    assert depth(130, pressure_tolerance=1e-3, pressure_max_iterations=100) == 8
+    assert depth(130, sweeps_per_pass=5) == 5
