@@ -360,42 +360,68 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         // normal component), corners keep their input value.
         const float h = F.h;
         int bad = 0;
+        // Rows go in batches of EB: first the cell each row reads u and v from (its own,
+        // or its inner neighbour's on an edge) for the whole batch, so the global loads
+        // are in flight together, then the arithmetic, in the reference's order.
+        constexpr int EB = SR / 2;
     #pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i, gr = gy0 + r;
-            if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
-            const bool row_int = gr >= 1 && gr <= rows - 2;
-            int ir = gr, ic = gc;
-            float su = 1.f, sv = 1.f;
-            bool corner = false;
-            if (col_int && row_int) {
-            } else if (row_int) {  // left / right edge
-                ic = (gc == 0) ? 1 : cols - 2;
-                su = -1.f;
-            } else if (col_int) {  // top / bottom edge
-                ir = (gr == 0) ? 1 : rows - 2;
-                sv = -1.f;
-            } else {
-                corner = true;
-            }
-            const size_t o = (size_t)gr * pitch + gc;
-            float un, vn;
-            if (corner) {
-                un = __ldcg(F.u_in + o);
-                vn = __ldcg(F.v_in + o);
-            } else {
-                const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
-                const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
-                const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
-                const float gu = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rr * RW + rcr], S[co + rr * RW + rcl])), h);
-                const float gv = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rrd * RW + rc], S[co + rru * RW + rc])), h);
+        for (int i0 = 0; i0 < SR; i0 += EB) {
+            float uin[EB], vin[EB];
+            unsigned live_rows = 0;
+    #pragma unroll
+            for (int k = 0; k < EB; ++k) {
+                const int r = r0 + i0 + k, gr = gy0 + r;
+                uin[k] = vin[k] = 0.f;
+                if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
+                const bool row_int = gr >= 1 && gr <= rows - 2;
+                int ir = gr, ic = gc;
+                if (!(col_int && row_int)) {
+                    if (row_int) ic = (gc == 0) ? 1 : cols - 2;       // left / right edge
+                    else if (col_int) ir = (gr == 0) ? 1 : rows - 2;  // top / bottom edge
+                }
                 const size_t oi = (size_t)ir * pitch + ic;
-                un = su * __fsub_rn(__ldcg(F.u_in + oi), gu);
-                vn = sv * __fsub_rn(__ldcg(F.v_in + oi), gv);
+                uin[k] = __ldcg(F.u_in + oi);
+                vin[k] = __ldcg(F.v_in + oi);
+                live_rows |= 1u << k;
             }
-            F.u_out[o] = un;
-            F.v_out[o] = vn;
-            bad |= !(isfinite(un) && isfinite(vn));
+    #pragma unroll
+            for (int k = 0; k < EB; ++k) {
+                if (!((live_rows >> k) & 1u)) continue;
+                const int r = r0 + i0 + k, gr = gy0 + r;
+                const bool row_int = gr >= 1 && gr <= rows - 2;
+                int ir = gr, ic = gc;
+                float su = 1.f, sv = 1.f;
+                bool corner = false;
+                if (col_int && row_int) {
+                } else if (row_int) {  // left / right edge
+                    ic = (gc == 0) ? 1 : cols - 2;
+                    su = -1.f;
+                } else if (col_int) {  // top / bottom edge
+                    ir = (gr == 0) ? 1 : rows - 2;
+                    sv = -1.f;
+                } else {
+                    corner = true;
+                }
+                const size_t o = (size_t)gr * pitch + gc;
+                float un, vn;
+                if (corner) {
+                    un = uin[k];
+                    vn = vin[k];
+                } else {
+                    const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
+                    const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
+                    const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
+                    const float gu =
+                        __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rr * RW + rcr], S[co + rr * RW + rcl])), h);
+                    const float gv =
+                        __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rrd * RW + rc], S[co + rru * RW + rc])), h);
+                    un = su * __fsub_rn(uin[k], gu);
+                    vn = sv * __fsub_rn(vin[k], gv);
+                }
+                F.u_out[o] = un;
+                F.v_out[o] = vn;
+                bad |= !(isfinite(un) && isfinite(vn));
+            }
         }
         if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
     }
