@@ -1349,22 +1349,13 @@ int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const
 
 }  // namespace
 
-int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate, float* u,
-                  float* v, const float* u_source, const float* v_source, float viscosity, float dt) {
-    if (!s || !density || !density_source || !u || !v || !u_source || !v_source)
-        return fail(FS_ERR_ARG, "fs_solve_host: null argument");
-    DeviceGuard g(s->device);
-    int rc;
-    if (s->cfg.method == FS_METHOD_JACOBI && (long)s->rows * s->cols >= FS_OVERLAP_MIN_CELLS) {
-        const float* host[6] = {density, u, v, density_source, u_source, v_source};
-        float* const out[3] = {density, u, v};
-        if ((rc = solve_host_overlapped(s, host, out, diffusion_rate, viscosity, dt)) != FS_OK) return rc;
-        CK(cudaStreamSynchronize(s->stream));
-        return check_flags(s);
-    }
-    // stage the six inputs densely in scratch fields the step overwrites anyway, then
-    // spread them into the pitched state and source fields with one kernel
-    const float* host[6] = {density, u, v, density_source, u_source, v_source};
+namespace {
+
+// One step on host grids without overlap (small grids): stage the six inputs densely in
+// scratch fields the step overwrites anyway, spread them into the pitched state and
+// source fields with one kernel, step (one graph launch), copy the state out.
+int solve_host_serial(fs_solver* s, const float* const host[6], float* const out[3], float diff, float visc,
+                      float dt) {
     float* stage[6] = {s->x0[0], s->x0[1], s->x0[2], s->pp[0][0], s->pp[1][0], s->pp[2][0]};
     Repack6 R;
     const size_t bytes = (size_t)s->rows * s->cols * sizeof(float);
@@ -1381,10 +1372,33 @@ int fs_solve_host(fs_solver* s, float* density, const float* density_source, flo
     repack_kernel<<<dim3(152 * 2, 6), 256, 0, s->stream>>>(R, s->rows, s->cols, s->pitch);
     CK(cudaGetLastError());
     s->stats.kernel_launches++;
-    if ((rc = run_steps(s, diffusion_rate, viscosity, dt, 1)) != FS_OK) return rc;
-    if ((rc = copy_out(s, density, s->st[F_D])) || (rc = copy_out(s, u, s->st[F_U])) ||
-        (rc = copy_out(s, v, s->st[F_V])))
+    int rc;
+    if ((rc = run_steps(s, diff, visc, dt, 1)) != FS_OK) return rc;
+    if ((rc = copy_out(s, out[0], s->st[F_D])) || (rc = copy_out(s, out[1], s->st[F_U])) ||
+        (rc = copy_out(s, out[2], s->st[F_V])))
         return rc;
+    return FS_OK;
+}
+
+}  // namespace
+
+int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate, float* u,
+                  float* v, const float* u_source, const float* v_source, float viscosity, float dt) {
+    if (!s || !density || !density_source || !u || !v || !u_source || !v_source)
+        return fail(FS_ERR_ARG, "fs_solve_host: null argument");
+    DeviceGuard g(s->device);
+    const float* host[6] = {density, u, v, density_source, u_source, v_source};
+    float* const out[3] = {density, u, v};
+    const bool overlap = s->cfg.method == FS_METHOD_JACOBI && (long)s->rows * s->cols >= FS_OVERLAP_MIN_CELLS;
+    const int rc = overlap ? solve_host_overlapped(s, host, out, diffusion_rate, viscosity, dt)
+                           : solve_host_serial(s, host, out, diffusion_rate, viscosity, dt);
+    if (rc != FS_OK) {
+        // copies from or into the caller's buffers may still be queued on any of the
+        // handle's streams: let them finish before the caller gets control back
+        for (cudaStream_t x : {s->xfer[0], s->xfer[1], s->side, s->stream})
+            if (x) cudaStreamSynchronize(x);
+        return rc;
+    }
     CK(cudaStreamSynchronize(s->stream));
     return check_flags(s);
 }
