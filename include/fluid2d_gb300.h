@@ -168,7 +168,11 @@ FS_API const char* fs_last_error(void);
 /* Replaces fluid_solver_gpu::solve (fluid_solver_gpu.cu:222-258), argument for
  * argument: uploads density/u/v and the three source grids from host memory, runs one
  * step, downloads density/u/v, and returns when they are written. Host buffers may be
- * pageable; pinned buffers (fs_host_alloc) copy faster. */
+ * pageable; pinned buffers (fs_host_alloc) copy faster. On grids of 2^20 cells and more
+ * the copies overlap the step (density first and diffusing while u and v upload; the new
+ * density downloading while the velocity is projected); the results are those of
+ * fs_upload + fs_upload_sources + fs_step + fs_download. On failure no copy from or into
+ * the host buffers is still in flight when the call returns. */
 FS_API int fs_solve_host(fs_solver* s, float* density, const float* density_source, float diffusion_rate,
                   float* u, float* v, const float* u_source, const float* v_source, float viscosity,
                   float dt);
