@@ -91,6 +91,7 @@ SIGNATURES = {
     "fs_step": (C.c_int, [_P, _F, _F, _F, _I]),
     "fs_download": (C.c_int, [_P, _P, _P, _P]),
     "fs_sync": (C.c_int, [_P]),
+    "fs_set_barrier_poll_limit": (C.c_int, [_P, C.c_uint]),
     "fs_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
     "fs_device_view_get": (C.c_int, [_P, C.POINTER(fs_device_view)]),
     "fs_stage": (C.c_int, [_P, _I, _F, _F]),
@@ -273,6 +274,10 @@ class Solver:
 
     def sync(self):
         _check(self._lib.fs_sync(self._h))
+
+    def set_barrier_poll_limit(self, polls: int):
+        """Bound of the residual solve's grid-barrier wait, in polls (0 = default)."""
+        _check(self._lib.fs_set_barrier_poll_limit(self._h, int(polls)))
 
     def solve(self, density, density_src, diffusion_rate, u, v, u_src, v_src, viscosity, dt):
         """fluid_solver::solve: one step on host grids, density/u/v updated in place."""

@@ -97,6 +97,8 @@ struct PressureSolve {
     int max_passes;
     int segment;                    // 1: segment mode
     float* p_cur;                   // segment: start and final pressure
+    const unsigned* poll_limit;     // device word: polls before a grid barrier gives up
+                                    // (0 or null = the default, about 2 s)
 };
 
 // Semi-Lagrangian advection parameters.

@@ -2,12 +2,11 @@
 // memory.
 //
 // Who needs it: code that calls the solver from inside a host framework that owns all
-// device memory (a fixed pool or budget, no raw cudaMalloc allowed), code that issues
-// the projection while a stream capture is being recorded (cudaMalloc is not a
-// stream-ordered call, so it is not allowed inside a global-mode capture), and frame
-// loops that must not allocate after start-up so they can neither stall on the
-// allocator nor fail with out-of-memory mid-run. fs_create() allocates the solver's
-// scratch with cudaMalloc, so these callers cannot use a handle.
+// device memory (a fixed pool or budget, no raw cudaMalloc allowed), plug-ins whose host
+// application hands them device buffers but no allocator, and frame loops that must not
+// allocate after start-up so they can neither stall on the allocator nor fail with
+// out-of-memory mid-run. fs_create() allocates the solver's scratch with cudaMalloc, so
+// these callers cannot use a handle.
 //
 // This entry point takes the caller's device buffers for its inputs and outputs and
 // keeps its own scratch (the divergence and two pressure buffers) in one file-scope
@@ -18,7 +17,9 @@
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (and sets the kernels' shared-memory limit) and caches it for
-// that device; make that first call before any stream capture. Every call shares the
+// that device; make that first call before any stream capture. A cudaDeviceReset() on a
+// device releases the array and leaves the cached address stale: calls on that device
+// after a reset are not supported. Every call shares the
 // one array: calls that can overlap on the GPU (different streams, or different host
 // threads on the same device) race on it and must be serialised by the caller. The
 // array keeps the previous call's contents; nothing in it needs to start at zero (the
@@ -29,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <mutex>
 #include <vector>
 
@@ -80,8 +82,20 @@ extern "C" int fs_project_noalloc(const float* u, const float* v, float* u_out, 
         return record_error(FS_ERR_ARG,
                             "fs_project_noalloc: rows * pitch exceeds FS_NOALLOC_MAX_CELLS (1048576 floats); "
                             "use a solver handle for larger grids");
-    if (u_out == u || u_out == v || v_out == u || v_out == v || u_out == v_out)
-        return record_error(FS_ERR_ARG, "fs_project_noalloc: outputs must not alias the inputs or each other");
+    // The last pass reads u and v around each output cell while other CTAs write the
+    // outputs, so no output may overlap an input or the other output anywhere in its
+    // rows x pitch extent (the inputs may overlap each other: they are only read).
+    {
+        const size_t extent = (size_t)rows * (size_t)pitch * sizeof(float);
+        auto overlap = [extent](const void* a, const void* b) {
+            const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+            return x < y + extent && y < x + extent;
+        };
+        if (overlap(u_out, u) || overlap(u_out, v) || overlap(v_out, u) || overlap(v_out, v) || overlap(u_out, v_out))
+            return record_error(FS_ERR_ARG,
+                                "fs_project_noalloc: an output overlaps an input or the other output (rows * pitch "
+                                "floats each)");
+    }
 
     float* base = nullptr;
     int rc = scratch_for_current_device(&base);

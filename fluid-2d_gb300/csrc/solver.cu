@@ -96,7 +96,7 @@ struct fs_solver {
     float* p[2] = {};
     float* vel1[2] = {};
     float* pwarm[2] = {};
-    int* flags = nullptr;  // [0]: non-finite
+    int* flags = nullptr;  // [0]: non-finite; [1]: grid-barrier poll limit of the residual solves (0 = default)
     // residual-driven pressure solves: one control block per projection of a step,
     // and the per-CTA residual partial sums of the persistent kernel
     SolveCtrl* ctrl = nullptr;
@@ -577,6 +577,7 @@ int enqueue_project_learned_cycles(fs_solver* s, const float* u_in, const float*
     P.p[1] = s->p[1];
     P.partials = s->partials[slot];
     P.ctrl = s->ctrl + slot;
+    P.poll_limit = reinterpret_cast<const unsigned*>(s->flags + 1);
     P.tol = s->cfg.pressure_tolerance;
     P.segment = 1;
     P.p_cur = pcur;
@@ -643,6 +644,7 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
     P.p_out = warm ? s->pwarm[slot] : nullptr;
     P.partials = s->partials[slot];
     P.ctrl = s->ctrl + slot;
+    P.poll_limit = reinterpret_cast<const unsigned*>(s->flags + 1);
     P.tol = s->cfg.pressure_tolerance;
     P.max_passes = std::max(1, (s->cfg.pressure_max_iterations + K - 1) / K);
     CK(cudaMemsetAsync(P.ctrl, 0, sizeof(SolveCtrl), s->stream));
@@ -1270,6 +1272,15 @@ int fs_sync(fs_solver* s) {
     DeviceGuard g(s->device);
     CK(cudaStreamSynchronize(s->stream));
     return check_flags(s);
+}
+
+int fs_set_barrier_poll_limit(fs_solver* s, unsigned polls) {
+    if (!s) return fail(FS_ERR_ARG, "fs_set_barrier_poll_limit: null handle");
+    DeviceGuard g(s->device);
+    // a device word read by every residual solve at launch, so captured step graphs see it too
+    CK(cudaMemcpyAsync(s->flags + 1, &polls, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FS_OK;
 }
 
 // Grids of at least this many cells take the overlapped host step below. On smaller

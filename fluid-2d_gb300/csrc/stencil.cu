@@ -7,21 +7,23 @@
 //     Kp x (copy, Jacobi, fill), gradient subtract, two reflecting fills.
 // That is ~20 B/cell of HBM traffic and two launches per sweep. Here one launch runs
 // `sweeps` sweeps of one or more fields: each CTA loads a 128-column region (its
-// output tile grown by a halo H >= sweeps), iterates in shared memory with the
+// output tile grown by a halo H >= sweeps), iterates on chip with the
 // boundary fill's effect reproduced exactly after every sweep, and writes only its
 // output tile back. The first pass of a solve fuses what precedes it
 // (add_sources for diffusion, the divergence for pressure) and the last pressure
 // pass fuses the gradient subtract and the two reflecting fills.
 //
-// Each thread owns one column of SR consecutive rows and keeps its constant terms
-// (x0 or div) in registers; every sweep streams down the column from the shared copy
-// of the previous sweep (double-buffered, one barrier per sweep) as two rolling
-// windows in lockstep, so each pair of cell updates issues as packed f32x2
-// instructions. The reference's per-sweep boundary fill is folded into the sweep (the
-// cells next to a domain edge read what the fill would have stored there) and applied
-// for real once, after the last sweep. All arithmetic uses
-// explicit round-to-nearest intrinsics in the reference's operand order, so no FMA
-// contraction changes its rounding (the one multiply feeding an add stays scalar). The reference divides by (1.0 + 4.0*a) in
+// The sweeps are register-blocked (run_sweeps): each thread holds an 8 x 4 block of
+// the field in registers, exchanges block edges with its neighbours by warp shuffles
+// and a small shared-memory row exchange, and reads its constant terms (x0 or div) from
+// shared memory, one barrier per sweep. Loads, stores and the fused first/last-pass
+// arithmetic use a one-column-per-thread layout for coalesced global access. The
+// reference's per-sweep boundary fill is folded into the sweep (the cells next to a
+// domain edge read what the fill would have stored there) and applied for real once,
+// after the last sweep. Arithmetic follows the reference's operand order with explicit
+// round-to-nearest intrinsics and a fused multiply-add exactly where the reference's
+// compiled kernels fuse one (add_sources x + dt*s and the diffusion numerator
+// x0 + a*sum). The reference divides by (1.0 + 4.0*a) in
 // double; FP64 is slow on GB300, so the quotient is formed as
 //   q = num*rf;  e = fma(-q, dh, num);  e = fma(-q, dl, e);  q = fma(e, rf, q)
 // with dh + dl = 1 + 4a split into two floats and rf = (float)(1/(1 + 4a)). This
@@ -38,11 +40,12 @@ namespace {
 
 __device__ __forceinline__ float diffuse_update(float x0, float L, float R, float U, float D, float a,
                                                 float dh, float dl, float rf) {
-    // (x0 + a*(L + R + U + D)) / (1 + 4a), fluid_solver_gpu.cu:81-82
+    // (x0 + a*(L + R + U + D)) / (1 + 4a), fluid_solver_gpu.cu:81-82; the compiled
+    // reference fuses x0 + a*sum into one FMA
     float s = __fadd_rn(L, R);
     s = __fadd_rn(s, U);
     s = __fadd_rn(s, D);
-    const float num = __fadd_rn(x0, __fmul_rn(a, s));
+    const float num = __fmaf_rn(a, s, x0);
     float q = __fmul_rn(num, rf);
     float e = __fmaf_rn(-q, dh, num);
     e = __fmaf_rn(-q, dl, e);
@@ -58,110 +61,95 @@ __device__ __forceinline__ float pressure_update(float dv, float L, float R, flo
     return __fmul_rn(s, 0.25f);
 }
 
-// The same updates on two cells at once with the packed FP32 pipe (sm_100+): each lane
-// of a float2 rounds exactly as the scalar form, so results are bit-identical; -q*dh is
-// written q*(-dh), the same exact product.
-__device__ __forceinline__ float2 diffuse_update2(float2 x0, float2 L, float2 R, float2 U, float2 D, float2 a,
-                                                  float2 ndh, float2 ndl, float2 rf) {
-    float2 s = __fadd2_rn(L, R);
-    s = __fadd2_rn(s, U);
-    s = __fadd2_rn(s, D);
-    // x0 + a*s with two roundings, as the reference: formed lane by lane, because the
-    // compiler may fuse a packed multiply feeding a packed add into one FFMA2
-    const float2 num = make_float2(__fadd_rn(x0.x, __fmul_rn(a.x, s.x)), __fadd_rn(x0.y, __fmul_rn(a.y, s.y)));
-    const float2 q = __fmul2_rn(num, rf);
-    float2 e = __ffma2_rn(q, ndh, num);
-    e = __ffma2_rn(q, ndl, e);
-    return __ffma2_rn(e, rf, q);
-}
-
-__device__ __forceinline__ float2 pressure_update2(float2 dv, float2 L, float2 R, float2 U, float2 D) {
-    float2 s = __fadd2_rn(dv, R);
-    s = __fadd2_rn(s, L);
-    s = __fadd2_rn(s, D);
-    s = __fadd2_rn(s, U);
-    return __fmul2_rn(s, make_float2(0.25f, 0.25f));
-}
-
-// All sweeps of one tile. Each thread owns one column of SR rows of the region and
-// keeps only its constant term (x0 or div) in registers: every sweep streams down the
-// column with a rolling up/centre/down window read from `cur` (the previous sweep) plus
-// the left and right neighbours, and writes the new value to `nxt` — three shared loads
-// and one store per cell update, and no per-row state carried across sweeps. One
-// barrier per sweep.
-//   EDGE = false: the region lies inside the domain interior; every cell updates, no
-//                 checks (cells near the region border compute values that nothing
-//                 stored depends on).
-//   EDGE = true:  bit i of `live` marks interior cells (others keep their value). The
-//                 reference fills the domain-edge cells after every sweep with their
-//                 inner neighbour's new value times a sign (set_boundary_*,
-//                 fluid_solver_gpu.cu:11-54), and the only cells that read an edge cell
-//                 are those inner neighbours. So from the second sweep on, an interior
-//                 cell next to an edge reads sign * (its own current value) in place of
-//                 the edge cell — the same float the fill would have stored there — and
-//                 the edge cells themselves are filled once, after the last sweep, by
-//                 fill_edges. The first sweep reads the edge cells as loaded.
-//                 up_bits / dn_bits: bit i set where row r0 + i is grid row 1 / rows - 2
-//                 (its upper / lower neighbour is an edge cell); at_left / at_right: this
-//                 column is grid column 1 / cols - 2.
-template <bool DIFF, bool EDGE, int SR, int RH>
-__device__ __forceinline__ void run_sweeps(const float2 (&k2)[SR / 2], int& co, int& no, int nsweeps, int r0,
-                                           int tx, int txl, int txr, unsigned live, unsigned up_bits,
-                                           unsigned dn_bits, bool at_left, bool at_right, float s_lr, float s_tb,
-                                           float a, float dh, float dl, float rf) {
-    constexpr int RW = kRegionW, H2 = SR / 2;
+// All sweeps of one tile, register-blocked. The region's RH x 128 cells are split
+// among the CTA's NW warps: warp w owns rows [w*SRB, w*SRB + SRB), and lane l of a
+// warp owns the four columns 4l .. 4l+3 of those rows, so each thread holds a
+// SRB x 4 block of the field (x) in registers for the whole pass; the constant term
+// (x0 or div) stays in shared memory at koff and is read as one float4 per row. Per
+// sweep and row, the left neighbour of column 0 and the right neighbour of column 3
+// come from the adjacent lanes by warp shuffles, and the rows above and below the block
+// from the adjacent warps through a small double-buffered exchange area at eoff (two
+// rows per warp, written and read as float4); everything else is in the thread's own
+// registers. Per 128 cell updates of a warp that is 2 shuffles, 4 wavefronts of
+// constant loads and 4 * 4 / SRB wavefronts of row exchange, against 16 wavefronts of
+// shared loads and stores for a one-column-per-thread rolling window (three loads and
+// one store per update). One barrier per sweep.
+// Cells at the region border read clamped or wrapped neighbours and compute values that
+// nothing stored depends on (the halo is at least the number of sweeps).
+//   EDGE = false: the region lies inside the domain interior; every cell updates.
+//   EDGE = true:  only interior cells update (row_int / col_int bits), the others keep
+//                 their value. The reference fills the domain-edge cells after every
+//                 sweep with their inner neighbour's new value times a sign
+//                 (set_boundary_*, fluid_solver_gpu.cu:11-54), and the only cells that
+//                 read an edge cell are those inner neighbours. So from the second sweep
+//                 on, an interior cell next to an edge reads sign * (its own current
+//                 value) in place of the edge cell, the same float the fill would have
+//                 stored there, and the edge cells themselves are filled once, after the
+//                 last sweep (fill_edges). The first sweep reads the edge cells as
+//                 loaded. i1 / i2: block row of grid row 1 / rows - 2 (or out of range);
+//                 q1 / q2: block column of grid column 1 / cols - 2 (or out of range).
+template <bool DIFF, bool EDGE, int NW, int SRB>
+__device__ __forceinline__ void run_sweeps(float (&x)[SRB][4], int koff, int eoff, int nsweeps, int w, int lane, unsigned row_int, unsigned col_int, int i1,
+                                           int i2, int q1, int q2, float s_lr, float s_tb, float a, float dh, float dl,
+                                           float rf) {
+    constexpr int RW = kRegionW;
+    constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ float4 smem4[];
-    float* const S = reinterpret_cast<float*>(smem4);
-    // offsets from this thread's first cell: the row above (clamped at the region top),
-    // the row below the last (clamped at the bottom), the left and right neighbours
-    // (clamped at the region sides); the clamped cells compute values nothing uses
-    const int up_off = r0 > 0 ? -RW : 0;
-    const int dn_off = (r0 + SR < RH) ? SR * RW : (SR - 1) * RW;
-    const int l_off = txl - tx, r_off = txr - tx;
-    const int base = r0 * RW + tx;
-    const float2 a2 = make_float2(a, a), ndh2 = make_float2(-dh, -dh), ndl2 = make_float2(-dl, -dl);
-    const float2 rf2 = make_float2(rf, rf);
+    float* const E = reinterpret_cast<float*>(smem4) + eoff;
+    const float* const K = reinterpret_cast<const float*>(smem4) + koff + (w * SRB) * RW + 4 * lane;
+    const int my_top = (2 * w) * RW + 4 * lane;
+    const int my_bot = my_top + RW;
+    // bottom row of warp w - 1 and top row of warp w + 1; the first and last warps read
+    // their own rows instead (the region border, whose values nothing stored uses)
+    const int nb_up = w > 0 ? my_top - RW : my_top;
+    const int nb_dn = w < NW - 1 ? my_top + 2 * RW : my_bot;
+    constexpr int EB = 2 * NW * RW;     // floats per exchange buffer
 #pragma unroll 1
     for (int s = 0; s < nsweeps; ++s) {
-        const float* __restrict__ c = S + co + base;
-        const float* __restrict__ cl = c + l_off;
-        const float* __restrict__ cr = c + r_off;
-        float* __restrict__ nx = S + no + base;
-        // edge folding starts with the second sweep
-        const unsigned ub = s > 0 ? up_bits : 0u, db = s > 0 ? dn_bits : 0u;
-        const bool fl = s > 0 && at_left, fr = s > 0 && at_right;
-        // two rolling windows down the segment in lockstep: rows j (x) and j + SR/2 (y)
-        float2 up = make_float2(c[up_off], c[(H2 - 1) * RW]);
-        float2 ce = make_float2(c[0], c[H2 * RW]);
-#pragma unroll
-        for (int j = 0; j < H2; ++j) {
-            const float2 dn = make_float2(c[(j + 1) * RW], j + 1 + H2 < SR ? c[(j + 1 + H2) * RW] : c[dn_off]);
-            float2 Lv = make_float2(cl[j * RW], cl[(j + H2) * RW]);
-            float2 Rv = make_float2(cr[j * RW], cr[(j + H2) * RW]);
-            float2 Dv = dn;
-            if (EDGE) {
-                if ((ub >> j) & 1u) up.x = __fmul_rn(s_tb, ce.x);
-                if ((ub >> (j + H2)) & 1u) up.y = __fmul_rn(s_tb, ce.y);
-                if ((db >> j) & 1u) Dv.x = __fmul_rn(s_tb, ce.x);
-                if ((db >> (j + H2)) & 1u) Dv.y = __fmul_rn(s_tb, ce.y);
-                if (fl) Lv = make_float2(__fmul_rn(s_lr, ce.x), __fmul_rn(s_lr, ce.y));
-                if (fr) Rv = make_float2(__fmul_rn(s_lr, ce.x), __fmul_rn(s_lr, ce.y));
-            }
-            float2 nv = DIFF ? diffuse_update2(k2[j], Lv, Rv, up, Dv, a2, ndh2, ndl2, rf2)
-                             : pressure_update2(k2[j], Lv, Rv, up, Dv);
-            if (EDGE) {
-                nv.x = ((live >> j) & 1u) ? nv.x : ce.x;
-                nv.y = ((live >> (j + H2)) & 1u) ? nv.y : ce.y;
-            }
-            nx[j * RW] = nv.x;
-            nx[(j + H2) * RW] = nv.y;
-            up = ce;
-            ce = dn;
-        }
+        const int eo = (s & 1) * EB;
+        *reinterpret_cast<float4*>(E + my_top + eo) = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
+        *reinterpret_cast<float4*>(E + my_bot + eo) = make_float4(x[SRB - 1][0], x[SRB - 1][1], x[SRB - 1][2],
+                                                              x[SRB - 1][3]);
         __syncthreads();
-        const int t = co;
-        co = no;
-        no = t;
+        float up[4], dn[4];
+        {
+            const float4 u4 = *reinterpret_cast<const float4*>(E + nb_up + eo);
+            const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn + eo);
+            up[0] = u4.x, up[1] = u4.y, up[2] = u4.z, up[3] = u4.w;
+            dn[0] = d4.x, dn[1] = d4.y, dn[2] = d4.z, dn[3] = d4.w;
+        }
+        const bool fold = EDGE && s > 0;
+        float prev[4] = {up[0], up[1], up[2], up[3]};  // previous sweep's row i - 1
+#pragma unroll
+        for (int i = 0; i < SRB; ++i) {
+            float cur[4], below[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                cur[q] = x[i][q];
+                below[q] = i + 1 < SRB ? x[i + 1][q] : dn[q];
+            }
+            const float lsh = __shfl_up_sync(FULL, cur[3], 1);
+            const float rsh = __shfl_down_sync(FULL, cur[0], 1);
+            const float4 k4 = *reinterpret_cast<const float4*>(K + i * RW);
+            const float kr[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float L = q > 0 ? cur[q - 1] : lsh;
+                float R = q < 3 ? cur[q + 1] : rsh;
+                float U = prev[q], D = below[q];
+                if (EDGE && fold) {
+                    if (i == i1) U = __fmul_rn(s_tb, cur[q]);
+                    if (i == i2) D = __fmul_rn(s_tb, cur[q]);
+                    if (q == q1) L = __fmul_rn(s_lr, cur[q]);
+                    if (q == q2) R = __fmul_rn(s_lr, cur[q]);
+                }
+                float nv = DIFF ? diffuse_update(kr[q], L, R, U, D, a, dh, dl, rf) : pressure_update(kr[q], L, R, U, D);
+                if (EDGE) nv = (((row_int >> i) & (col_int >> q)) & 1u) ? nv : cur[q];
+                x[i][q] = nv;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) prev[q] = cur[q];
+        }
     }
 }
 
@@ -219,20 +207,69 @@ __device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi,
     }
 }
 
+struct SweepParams {
+    int nsweeps, edge, gy0, gx0, rows, cols;
+    float s_lr, s_tb, a, dh, dl, rf;
+};
+
+// The sweeps of one tile in the block layout of run_sweeps: the field (X) and its
+// constant term (K) go from shared memory into registers, the sweeps run, and the final
+// field goes back to X. Kept out of line so that the tile body's other live values are
+// saved once around the call instead of competing with the register blocks.
+template <bool DIFF, int NW, int SRB>
+__device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P) {
+    constexpr int RW = kRegionW;
+    extern __shared__ float4 smem4[];
+    float* const X = reinterpret_cast<float*>(smem4) + xoff;
+    const int tid = threadIdx.y * RW + threadIdx.x;
+    const int w = tid >> 5, lane = tid & 31;
+    const int rb = w * SRB, cb = 4 * lane;
+    float xb[SRB][4];
+#pragma unroll
+    for (int i = 0; i < SRB; ++i) {
+        const float4 t = *reinterpret_cast<const float4*>(X + (rb + i) * RW + cb);
+        xb[i][0] = t.x, xb[i][1] = t.y, xb[i][2] = t.z, xb[i][3] = t.w;
+    }
+    __syncthreads();  // the exchange area of the sweeps overlays X
+    if (P.edge) {
+        const int gyb = P.gy0 + rb, gxb = P.gx0 + cb;
+        unsigned row_int = 0, col_int4 = 0;
+#pragma unroll
+        for (int i = 0; i < SRB; ++i) row_int |= (unsigned)(gyb + i >= 1 && gyb + i <= P.rows - 2) << i;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) col_int4 |= (unsigned)(gxb + q >= 1 && gxb + q <= P.cols - 2) << q;
+        run_sweeps<DIFF, true, NW, SRB>(xb, koff, xoff, P.nsweeps, w, lane, row_int, col_int4, 1 - gyb, P.rows - 2 - gyb,
+                                        1 - gxb, P.cols - 2 - gxb, P.s_lr, P.s_tb, P.a, P.dh, P.dl, P.rf);
+    } else {
+        run_sweeps<DIFF, false, NW, SRB>(xb, koff, xoff, P.nsweeps, w, lane, 0u, 0u, -1, -1, -1, -1, P.s_lr, P.s_tb, P.a,
+                                         P.dh, P.dl, P.rf);
+    }
+    __syncthreads();  // every warp has read its last exchange rows
+#pragma unroll
+    for (int i = 0; i < SRB; ++i)
+        *reinterpret_cast<float4*>(X + (rb + i) * RW + cb) = make_float4(xb[i][0], xb[i][1], xb[i][2], xb[i][3]);
+    __syncthreads();
+}
+
 // One tile of one pass: load the region (fusing add_sources or the divergence into
 // the first pass), run F.sweeps sweeps (edge CTAs: with the boundary fill folded in and
 // applied once at the end), store the
 // output tile, then the optional gradient-subtract epilogue and the optional residual
 // partial sums (for residual-driven pressure solves). xin/yout stand in for F.x/F.y so
 // a persistent caller can ping-pong buffers across passes.
-template <int TY, int SR, bool DIFF>
+template <int TY, int SRB, bool DIFF>
 __device__ __forceinline__ void process_tile(const StencilField& F, int b, const float* __restrict__ xin,
                                              float* __restrict__ yout, bool resid,
                                              float& rnum, float& rden) {
-    constexpr int RW = kRegionW, RH = TY * SR;
+    // Two thread layouts over the same region: the column layout (thread = one column,
+    // SR consecutive rows; coalesced global loads and stores, the fused first-pass
+    // arithmetic, the epilogues) and the block layout of run_sweeps.
+    constexpr int RW = kRegionW, NW = 4 * TY, RH = NW * SRB, SR = RH / TY;
+    static_assert(SR <= 32, "column-layout row masks are 32-bit");
+    static_assert(SRB >= 4, "the sweep exchange area must fit in one region buffer");
     extern __shared__ float4 smem4[];
     float* const S = reinterpret_cast<float*>(smem4);
-    int co = 0, no = RH * RW;  // offsets of the current / next sweep buffers in S
+    constexpr int co = 0, no = RH * RW;  // S + co: the field; S + no: its constant term
     __syncthreads();  // the previous tile of this CTA may still be reading shared memory
     int tyi, txi;
     tile_coords(b, F.tiles_x, F.tiles_y, tyi, txi);
@@ -249,9 +286,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txl = tx > 0 ? tx - 1 : 0;
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
 
-    float c[SR];
-    float2 k2[SR / 2];  // constant terms: row i in k2[i].x (i < SR/2) or k2[i - SR/2].y
-#define KREF(i) ((i) < SR / 2 ? k2[(i)].x : k2[(i) - SR / 2].y)
+#define KREF(i) (S[no + (r0 + (i)) * RW + tx])
+#define XREF(i) (S[co + (r0 + (i)) * RW + tx])
 
     // Row masks of this thread's column segment (bit i = row r0 + i of the region),
     // computed once so that the unrolled row loops below test one bit per row:
@@ -270,6 +306,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
                                                                          // only masked rows are dereferenced)
 
     // ------------------------------------------------------------------ load
+    // The field goes to S + co and its constant term to S + no, row by row.
     if (kind == PASS_PRESSURE_FIRST) {
         // divergence_kernel (fluid_solver_gpu.cu:173-174) on the region, from u, v
         // staged in the two shared buffers.
@@ -282,7 +319,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         }
         __syncthreads();
         const float cdiv = F.cdiv;
-        const float* __restrict__ cst = F.cst;
+        float kc[SR];
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
             const int r = r0 + i;
@@ -290,10 +327,16 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
             s = __fadd_rn(s, S[no + rd * RW + tx]);
             s = __fsub_rn(s, S[no + ru * RW + tx]);
-            KREF(i) = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
-            c[i] = (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
+            kc[i] = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
         }
         __syncthreads();
+        const float* __restrict__ cst = F.cst;  // starting pressure (null = zero)
+#pragma unroll
+        for (int i = 0; i < SR; ++i) {
+            S[co + (r0 + i) * RW + tx] =
+                (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
+            S[no + (r0 + i) * RW + tx] = kc[i];
+        }
     } else if (kind == PASS_DIFFUSE_FIRST) {
         // add_sources_kernel (fluid_solver_gpu.cu:64) fused into the load
         const float dt = F.dt;
@@ -301,38 +344,28 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
             float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            if ((m_int >> i) & 1u) x = __fadd_rn(x, __fmul_rn(dt, __ldcg(F.x2 + o)));
-            c[i] = x;
-            KREF(i) = x;
+            if ((m_int >> i) & 1u) x = __fmaf_rn(dt, __ldcg(F.x2 + o), x);  // fused, as compiled
+            S[co + (r0 + i) * RW + tx] = x;
+            S[no + (r0 + i) * RW + tx] = x;
         }
     } else {
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
-            c[i] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            KREF(i) = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
+            S[co + (r0 + i) * RW + tx] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
+            S[no + (r0 + i) * RW + tx] = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
         }
     }
-#pragma unroll
-    for (int i = 0; i < SR; ++i) S[co + (r0 + i) * RW + tx] = c[i];
     __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
-    if (edge_cta) {
-        const int i1 = 1 - g0, i2 = rows - 2 - g0;  // segment rows of grid rows 1 and rows - 2
-        const unsigned up_bits = (i1 >= 0 && i1 < SR) ? 1u << i1 : 0u;
-        const unsigned dn_bits = (i2 >= 0 && i2 < SR) ? 1u << i2 : 0u;
-        run_sweeps<DIFF, true, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, m_int, up_bits, dn_bits, gc == 1,
-                                       gc == cols - 2, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf);
-        if (F.sweeps > 0) fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
-    } else {
-        run_sweeps<DIFF, false, SR, RH>(k2, co, no, F.sweeps, r0, tx, txl, txr, 0u, 0u, 0u, false, false, F.s_lr,
-                                        F.s_tb, F.a, F.dh, F.dl, F.rf);
+    if (F.sweeps > 0) {
+        const SweepParams P = {F.sweeps, edge_cta ? 1 : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        sweep_phase<DIFF, NW, SRB>(co, no, P);
+        if (edge_cta) fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
     }
-    // final values of this thread's column (S + co is complete after the last barrier)
-#pragma unroll
-    for (int i = 0; i < SR; ++i) c[i] = S[co + (r0 + i) * RW + tx];
+    // final values of this thread's column: XREF(i) (S + co is complete after the last barrier)
 
     // ------------------------------------------------------------------ store
     const bool col_out = col_in && tx >= H && tx < H + F.tile_w;
@@ -343,7 +376,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         if (y) {
 #pragma unroll
             for (int i = 0; i < SR; ++i)
-                if ((m_out >> i) & 1u) y[o0 + (size_t)i * pitch] = c[i];
+                if ((m_out >> i) & 1u) y[o0 + (size_t)i * pitch] = XREF(i);
         }
         if (ko) {
 #pragma unroll
@@ -363,7 +396,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         // Rows go in batches of EB: first the cell each row reads u and v from (its own,
         // or its inner neighbour's on an edge) for the whole batch, so the global loads
         // are in flight together, then the arithmetic, in the reference's order.
-        constexpr int EB = SR / 2;
+        constexpr int EB = 8;
     #pragma unroll
         for (int i0 = 0; i0 < SR; i0 += EB) {
             float uin[EB], vin[EB];
@@ -439,7 +472,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             sres += S[co + r * RW + txl];
             sres += S[co + rd * RW + tx];
             sres += S[co + ru * RW + tx];
-            const float res = sres - 4.f * c[i];
+            const float res = sres - 4.f * XREF(i);
             rnum = fmaf(res, res, rnum);
             rden = fmaf(KREF(i), KREF(i), rden);
         }
@@ -447,27 +480,27 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 }
 
 #undef KREF
+#undef XREF
 
 // One launch = one pass over the tiles of up to kMaxStencilFields fields.
-template <int TY, int SR, bool DIFF>
-__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+template <int TY, int SRB, bool DIFF>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
     stencil_kernel(const __grid_constant__ StencilLaunch L) {
-    constexpr int RH = TY * SR;
-    extern __shared__ float4 smem4[];
+        extern __shared__ float4 smem4[];
     int b = blockIdx.x, f = 0;
 #pragma unroll 1
     while (f + 1 < L.nfields && b >= L.f[f + 1].tile_begin) ++f;
     const StencilField& F = L.f[f];
     float rn = 0.f, rd = 0.f;
-    process_tile<TY, SR, DIFF>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
+    process_tile<TY, SRB, DIFF>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
 }
 
 // One pass over a device-resident table of fields (a batch of grids of uneven size):
 // one CTA per tile of the concatenated tile list; tile_field[t] names the field of
 // tile t and prefix[f] its first tile. The field's descriptor is staged in shared
 // memory, where the tile body reads it many times.
-template <int TY, int SR, bool DIFF>
-__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+template <int TY, int SRB, bool DIFF>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
     stencil_table_kernel(const StencilField* __restrict__ tab, const int* __restrict__ prefix,
                          const int* __restrict__ tile_field) {
     __shared__ StencilField sF;
@@ -479,19 +512,19 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
         reinterpret_cast<int*>(&sF)[tid] = __ldg(reinterpret_cast<const int*>(tab + f) + tid);
     __syncthreads();
     float rn = 0.f, rd = 0.f;
-    process_tile<TY, SR, DIFF>(sF, t - __ldg(prefix + f), sF.x, sF.y, false, rn, rd);
+    process_tile<TY, SRB, DIFF>(sF, t - __ldg(prefix + f), sF.x, sF.y, false, rn, rd);
 }
 
 // ---------------------------------------------------------------------------
 // Residual-driven pressure solve in one persistent cooperative launch.
 
-constexpr unsigned kBarrierSpinLimit = 1u << 24;  // ~2 s of polling, then give up
+constexpr unsigned kBarrierSpinLimit = 1u << 24;  // default: ~2 s of polling, then give up
 
 // Grid-wide barrier for a cooperative launch (all CTAs co-resident). The wait is
-// bounded: after kBarrierSpinLimit polls the CTA sets ctrl->error and continues, and
-// every later barrier returns at once, so the kernel always terminates. Returns false
-// once an error has been flagged.
-__device__ __forceinline__ bool grid_barrier(SolveCtrl* ctrl, unsigned nblocks) {
+// bounded: after `limit` polls the CTA sets ctrl->error and continues, and every later
+// barrier returns at once, so the kernel always terminates. Returns false once an error
+// has been flagged.
+__device__ __forceinline__ bool grid_barrier(SolveCtrl* ctrl, unsigned nblocks, unsigned limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -506,7 +539,7 @@ __device__ __forceinline__ bool grid_barrier(SolveCtrl* ctrl, unsigned nblocks) 
         } else {
             unsigned spins = 0;
             while (*gen == g && *err == 0) {
-                if (++spins > kBarrierSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(&ctrl->error, 1);
                     break;
                 }
@@ -553,14 +586,14 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 
 // Out-of-line tile call for the persistent kernel: keeps the pass loop's state out
 // of the tile body's register budget.
-template <int TY, int SR>
+template <int TY, int SRB>
 __device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, bool resid,
                                            float& rn, float& rd) {
-    process_tile<TY, SR, false>(F, t, x, y, resid, rn, rd);
+    process_tile<TY, SRB, false>(F, t, x, y, resid, rn, rd);
 }
 
-template <int TY, int SR>
-__global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
+template <int TY, int SRB>
+__global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
     pressure_solve_kernel(const __grid_constant__ PressureSolve P) {
     const unsigned G = gridDim.x;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
@@ -572,6 +605,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     // segment mode, converged in an earlier segment: the flag was written by an earlier
     // launch, so every CTA reads the same value and none waits at a barrier
     if (P.segment && __ldcg(&P.ctrl->converged)) return;
+    const unsigned lim_set = P.poll_limit ? __ldcg(P.poll_limit) : 0u;
+    const unsigned limit = lim_set ? lim_set : kBarrierSpinLimit;
     int pass = 0;
 #pragma unroll 1
     for (; ok && !done && pass < P.max_passes; ++pass) {
@@ -581,7 +616,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
         float rn = 0.f, rd = 0.f;
 #pragma unroll 1
         for (int t = blockIdx.x; t < ntiles; t += G)
-            pressure_tile<TY, SR>(F, t, x, P.p[dst], true, rn, rd);
+            pressure_tile<TY, SRB>(F, t, x, P.p[dst], true, rn, rd);
         double a = rn, b = rd;
         block_sum2(a, b);
         double* part = P.partials + (size_t)(pass & 1) * 2 * G;
@@ -589,7 +624,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             part[2 * blockIdx.x] = a;
             part[2 * blockIdx.x + 1] = b;
         }
-        ok = grid_barrier(P.ctrl, G);
+        ok = grid_barrier(P.ctrl, G, limit);
         passes++;
         cur = dst;
         if (!ok) break;
@@ -617,7 +652,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
             float rn = 0.f, rd = 0.f;
 #pragma unroll 1
             for (int t = blockIdx.x; t < nfin; t += G)
-                pressure_tile<TY, SR>(P.fin, t, P.p[cur], P.p_out, false, rn, rd);
+                pressure_tile<TY, SRB>(P.fin, t, P.p[cur], P.p_out, false, rn, rd);
         }
     }
     if (blockIdx.x == 0 && tid == 0) {
@@ -627,81 +662,81 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 4 ? 2 : 1))
     }
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 constexpr size_t smem_bytes() {
-    return 2ull * TY * SR * kRegionW * sizeof(float);
+    return 2ull * (4 * TY * SRB) * kRegionW * sizeof(float);  // field + constant term
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 cudaError_t prepare_variant() {
-    const int smem = (int)smem_bytes<TY, SR>();
-    cudaError_t e = cudaFuncSetAttribute(stencil_kernel<TY, SR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const int smem = (int)smem_bytes<TY, SRB>();
+    cudaError_t e = cudaFuncSetAttribute(stencil_kernel<TY, SRB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(stencil_kernel<TY, SR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(stencil_kernel<TY, SRB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(pressure_solve_kernel<TY, SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(pressure_solve_kernel<TY, SRB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SRB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(stencil_table_kernel<TY, SRB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem);
     return e;
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 cudaError_t launch_table_variant(const StencilField* tab, const int* prefix, const int* tile_field, int total,
                                  bool diffuse, cudaStream_t st) {
     if (total <= 0) return cudaSuccess;
     if (diffuse)
-        stencil_table_kernel<TY, SR, true><<<total, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix,
+        stencil_table_kernel<TY, SRB, true><<<total, dim3(kRegionW, TY), smem_bytes<TY, SRB>(), st>>>(tab, prefix,
                                                                                                      tile_field);
     else
-        stencil_table_kernel<TY, SR, false><<<total, dim3(kRegionW, TY), smem_bytes<TY, SR>(), st>>>(tab, prefix,
+        stencil_table_kernel<TY, SRB, false><<<total, dim3(kRegionW, TY), smem_bytes<TY, SRB>(), st>>>(tab, prefix,
                                                                                                       tile_field);
     return cudaGetLastError();
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 cudaError_t solve_blocks(int* blocks) {
     int dev = 0, sms = 0, per = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pressure_solve_kernel<TY, SR>, kRegionW * TY,
-                                                          smem_bytes<TY, SR>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pressure_solve_kernel<TY, SRB>, kRegionW * TY,
+                                                          smem_bytes<TY, SRB>());
     *blocks = per * sms;
     return e;
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 cudaError_t launch_solve_variant(const PressureSolve& P, int blocks, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(kRegionW, TY);
-    cfg.dynamicSmemBytes = smem_bytes<TY, SR>();
+    cfg.dynamicSmemBytes = smem_bytes<TY, SRB>();
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, pressure_solve_kernel<TY, SR>, P);
+    return cudaLaunchKernelEx(&cfg, pressure_solve_kernel<TY, SRB>, P);
 }
 
-template <int TY, int SR>
+template <int TY, int SRB>
 cudaError_t launch_variant(const StencilLaunch& L, cudaStream_t st) {
-    const size_t smem = smem_bytes<TY, SR>();
+    const size_t smem = smem_bytes<TY, SRB>();
     int blocks = 0;
     for (int i = 0; i < L.nfields; ++i) blocks += L.f[i].tiles_x * L.f[i].tiles_y;
     if (blocks == 0) return cudaSuccess;
     // all fields of one launch are of the same class (diffusion or pressure)
     const bool diff = L.f[0].kind == PASS_DIFFUSE_FIRST || L.f[0].kind == PASS_DIFFUSE;
     if (diff)
-        stencil_kernel<TY, SR, true><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
+        stencil_kernel<TY, SRB, true><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
     else
-        stencil_kernel<TY, SR, false><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
+        stencil_kernel<TY, SRB, false><<<blocks, dim3(kRegionW, TY), smem, st>>>(L);
     return cudaGetLastError();
 }
 
@@ -712,31 +747,31 @@ int stencil_max_halo(int tile_rows) { return tile_rows / 2 - 2; }
 // Opt the kernels into more than 48 KB of dynamic shared memory on the current
 // device. Called once per handle at creation, outside any stream capture.
 cudaError_t stencil_prepare() {
-    cudaError_t e = prepare_variant<4, 16>();
-    if (e == cudaSuccess) e = prepare_variant<8, 16>();
+    cudaError_t e = prepare_variant<2, 8>();
+    if (e == cudaSuccess) e = prepare_variant<4, 8>();
     return e;
 }
 
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st) {
-    if (tile_rows == 128) return launch_variant<8, 16>(L, st);
-    return launch_variant<4, 16>(L, st);
+    if (tile_rows == 128) return launch_variant<4, 8>(L, st);
+    return launch_variant<2, 8>(L, st);
 }
 
 cudaError_t pressure_solve_max_blocks(int tile_rows, int* blocks) {
-    if (tile_rows == 128) return solve_blocks<8, 16>(blocks);
-    return solve_blocks<4, 16>(blocks);
+    if (tile_rows == 128) return solve_blocks<4, 8>(blocks);
+    return solve_blocks<2, 8>(blocks);
 }
 
 cudaError_t launch_pressure_solve(const PressureSolve& P, int tile_rows, int blocks, cudaStream_t st) {
     if (blocks <= 0) return cudaErrorInvalidValue;
-    if (tile_rows == 128) return launch_solve_variant<8, 16>(P, blocks, st);
-    return launch_solve_variant<4, 16>(P, blocks, st);
+    if (tile_rows == 128) return launch_solve_variant<4, 8>(P, blocks, st);
+    return launch_solve_variant<2, 8>(P, blocks, st);
 }
 
 cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, const int* tile_field, int total_tiles,
                                  bool diffuse, int tile_rows, cudaStream_t st) {
-    if (tile_rows == 128) return launch_table_variant<8, 16>(table, prefix, tile_field, total_tiles, diffuse, st);
-    return launch_table_variant<4, 16>(table, prefix, tile_field, total_tiles, diffuse, st);
+    if (tile_rows == 128) return launch_table_variant<4, 8>(table, prefix, tile_field, total_tiles, diffuse, st);
+    return launch_table_variant<2, 8>(table, prefix, tile_field, total_tiles, diffuse, st);
 }
 
 }  // namespace fs

@@ -175,6 +175,33 @@ def batch(count=256, seed=4, kd=30, kp=30, dt=0.05, rate=1e-5):
     return sims
 
 
+def portable_state(rows, cols, seed, coarse=32, vmax=0.2):
+    """Smooth seeded fields (d in [0, 1], u and v in +-vmax, reflecting walls) that every
+    host generates bit for bit: coarse uniform samples upsampled bilinearly with IEEE
+    +, -, * and / only, in a fixed order (no library transcendental whose last bit may
+    differ between x86 and Arm). Used where a fixture made on one machine is checked
+    against inputs regenerated on another."""
+    rng = np.random.default_rng(seed)
+    y = np.arange(rows, dtype=np.float64) * (coarse / (rows - 1.0))
+    x = np.arange(cols, dtype=np.float64) * (coarse / (cols - 1.0))
+    i0 = np.minimum(np.floor(y).astype(np.int64), coarse - 1)
+    j0 = np.minimum(np.floor(x).astype(np.int64), coarse - 1)
+    fy = (y - i0)[:, None]
+    fx = (x - j0)[None, :]
+
+    def field(lo, hi):
+        c = rng.uniform(lo, hi, size=(coarse + 1, coarse + 1))
+        top = c[i0][:, j0] * (1.0 - fx) + c[i0][:, j0 + 1] * fx
+        bot = c[i0 + 1][:, j0] * (1.0 - fx) + c[i0 + 1][:, j0 + 1] * fx
+        return np.ascontiguousarray((top * (1.0 - fy) + bot * fy).astype(np.float32))
+
+    d = field(0.0, 1.0)
+    u = field(-vmax, vmax)
+    v = field(-vmax, vmax)
+    reflect_boundaries(u, v)
+    return d, u, v
+
+
 def random_state(rows, cols, seed, vmax=1.0):
     """Unstructured random fields for kernel-level tests (odd sizes, tile edges)."""
     rng = np.random.default_rng(seed)

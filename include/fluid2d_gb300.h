@@ -185,6 +185,13 @@ FS_API int fs_step(fs_solver* s, float diffusion_rate, float viscosity, float dt
 FS_API int fs_download(fs_solver* s, float* density, float* u, float* v);
 FS_API int fs_sync(fs_solver* s);
 
+/* Bound of the grid-wide barrier wait in a residual-driven pressure solve
+ * (pressure_tolerance > 0), in polls of about 120 ns; 0 restores the default (2^24 polls,
+ * about 2 s). When a wait runs out the solve stops, the step's velocity is left
+ * unprojected and fs_sync / fs_step return FS_ERR_TIMEOUT; the handle stays usable.
+ * The reference has no bounded waits (it has no grid-wide synchronisation at all). */
+FS_API int fs_set_barrier_poll_limit(fs_solver* s, unsigned polls);
+
 FS_API int fs_get_stats(const fs_solver* s, fs_stats* out);
 FS_API int fs_device_view_get(fs_solver* s, fs_device_view* out);
 
@@ -285,22 +292,26 @@ FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, 
 /* Pressure projection that allocates nothing. No counterpart in the reference.
  *
  * For callers that cannot call cudaMalloc: code running inside a host framework that
- * owns all device memory, code issuing work while a stream capture is recorded
- * (cudaMalloc is not allowed inside a global-mode capture), and frame loops that must
- * not allocate after start-up. fs_create() allocates, so they cannot use a handle.
+ * owns all device memory (a fixed pool or budget), plug-ins whose host application hands
+ * them device buffers but no allocator, and frame loops that must not allocate after
+ * start-up. fs_create() allocates, so they cannot use a handle.
  *
- * Projects (u, v) -> (u_out, v_out) with `iterations` Jacobi sweeps from zero pressure,
- * exactly as a handle's projection stage (fluid_solver_gpu.cu:358-404 semantics). All
- * four arrays are the caller's device buffers of rows x pitch floats (element (i, j) at
- * i*pitch + j, rows/cols including the boundary); outputs must not alias inputs. Work is
- * queued on `stream` (a cudaStream_t; NULL = default stream) and is asynchronous.
+ * Projects (u, v) -> (u_out, v_out) with `iterations` Jacobi sweeps from zero pressure:
+ * the same result as fs_stage(FS_STAGE_PROJECT) on a handle created with
+ * pressure_iterations = iterations and warm_start = FS_WARM_ZERO. All four arrays are
+ * the caller's device buffers of rows x pitch floats (element (i, j) at i*pitch + j,
+ * rows/cols including the boundary); no output may overlap an input or the other output
+ * (FS_ERR_ARG). Work is queued on `stream` (a cudaStream_t; NULL = default stream) and is
+ * asynchronous.
  *
  * Scratch (divergence and two pressure buffers) lives in a fixed file-scope device
  * array of 3 x FS_NOALLOC_MAX_CELLS floats (12 MiB) that every GPU loading this library
  * holds until process exit; rows * pitch above FS_NOALLOC_MAX_CELLS is rejected with
  * FS_ERR_ARG. The first call on a device looks up that array's address and caches it:
- * make it before any stream capture. All calls share the array, so calls that may
- * overlap on the GPU race and must be serialised by the caller. */
+ * make it before any stream capture. After cudaDeviceReset() on a device the cached
+ * address is stale and further calls on that device are not supported. All calls share
+ * the array, so calls that may overlap on the GPU race and must be serialised by the
+ * caller. */
 #define FS_NOALLOC_MAX_CELLS 1048576
 FS_API int fs_project_noalloc(const float* u, const float* v, float* u_out, float* v_out, int rows, int cols,
                               int pitch, int iterations, void* stream);

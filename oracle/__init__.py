@@ -21,6 +21,7 @@ BND_CONT, BND_OPP_H, BND_OPP_V = 0, 1, 2
 
 _lib = None
 _ref = None
+_ref_gpu = None
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -49,6 +50,7 @@ def lib():
         L.orc_residual_f32.restype = C.c_double
         L.orc_residual_f64.argtypes = [_L, _L, _f64p, _f64p]
         L.orc_residual_f64.restype = C.c_double
+        L.orc_set_contract.argtypes = [_I, _I]
         _lib = L
     return _lib
 
@@ -67,6 +69,68 @@ def ref_lib():
         R.ref_cpu_solve.argtypes = [_L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I]
         _ref = R
     return _ref
+
+
+def ref_gpu_lib():
+    """The reference's own GPU kernels (oracle/_ref/ref_gpu.fatbin, compiled from the
+    reference's src/fluid_solver_gpu.cu) behind oracle/ref_gpu_runner.cpp, or None
+    where the fatbinary or a CUDA driver is absent. Needs a GPU to load."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        fat = _b.build_ref_gpu()
+        runner = _b.build_ref_gpu_runner()
+        if fat is None or runner is None or not fat.exists():
+            return None
+        try:
+            R = C.CDLL(str(runner))
+        except OSError:
+            return None
+        R.ref_gpu_last_error.restype = C.c_char_p
+        R.ref_gpu_load.argtypes = [C.c_char_p]
+        R.ref_gpu_solve.argtypes = [_L, _L, _f32p, _f32p, _F, _f32p, _f32p, _f32p, _f32p, _F, _F, _I, _I, _I]
+        R.ref_gpu_stage.argtypes = [_I, _L, _L, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _I, _F, _F, _I]
+        if R.ref_gpu_load(str(fat).encode()) != 0:
+            raise RuntimeError("reference GPU kernels failed to load: " + R.ref_gpu_last_error().decode())
+        _ref_gpu = R
+    return _ref_gpu
+
+
+def ref_gpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=15, kp=20, nsteps=1):
+    """The reference's GPU solver step (src/fluid_solver_gpu.cu:222-258) run by its own
+    compiled kernels, nsteps times with constant sources. The reference hard-codes
+    kd = 15, kp = 20; other counts run the same kernels with the given sweep counts."""
+    R = ref_gpu_lib()
+    if R is None:
+        raise RuntimeError("compiled reference GPU kernels unavailable")
+    d, ds, u, v, us, vs = (_c(a) for a in (d, ds, u, v, us, vs))
+    if R.ref_gpu_solve(d.shape[0], d.shape[1], d, ds, diff, u, v, us, vs, visc, dt, kd, kp, nsteps) != 0:
+        raise RuntimeError("reference GPU solve failed: " + R.ref_gpu_last_error().decode())
+    return d, u, v
+
+
+def set_contract(contract, bilinear=-1):
+    """Multiply-add fusion of the "gpu" restatement: contract=1 fuses where the
+    reference's compiled kernels fuse, with `bilinear` selecting the gather's pattern
+    (see oracle.cpp); contract=0 rounds every product and sum separately."""
+    lib().orc_set_contract(int(contract), int(bilinear))
+
+
+REF_ADD_SOURCES, REF_DIFFUSE, REF_ADVECT_TRACE, REF_SMOOTH, REF_ADVECT, REF_PROJECT = range(6)
+
+
+def ref_gpu_stage(stage, x=None, src=None, u=None, v=None, mode=0, rate=0.0, dt=0.0, iters=0):
+    """One helper of the reference's GPU solver (add_sources, diffuse, advect(trace),
+    smooth, advect, project; src/fluid_solver_gpu.cu:278-404) run by its own compiled
+    kernels. Returns the updated x, or (u, v) for project."""
+    R = ref_gpu_lib()
+    if R is None:
+        raise RuntimeError("compiled reference GPU kernels unavailable")
+    arrs = [None if a is None else _c(a) for a in (x, src, u, v)]
+    shape = next(a.shape for a in arrs if a is not None)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    if R.ref_gpu_stage(stage, shape[0], shape[1], *map(ptr, arrs), mode, rate, dt, iters) != 0:
+        raise RuntimeError("reference GPU stage failed: " + R.ref_gpu_last_error().decode())
+    return (arrs[2], arrs[3]) if stage == REF_PROJECT else arrs[0]
 
 
 def _c(a, dt=np.float32):
@@ -229,27 +293,35 @@ def render_velocity_lines(u, v, hscale, vscale):
     return out
 
 
+def script_sources(shape, events, k, step):
+    """Source grids of one step of a scripted run: the events of `step` (starting at
+    index k) added to zeroed grids in order, source(i, j) += value * width * height in
+    float32 (src/simulation.cpp:44-51). Returns (ds, us, vs, next k)."""
+    rows, cols = shape
+    w, h = np.float32(cols), np.float32(rows)
+    ds = np.zeros(shape, np.float32)
+    us = np.zeros(shape, np.float32)
+    vs = np.zeros(shape, np.float32)
+    while k < len(events) and events[k][0] == step:
+        _, kind, i, j, a, b = events[k]
+        if kind == 0:
+            ds[i, j] = np.float32(ds[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
+        else:
+            us[i, j] = np.float32(us[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
+            vs[i, j] = np.float32(vs[i, j] + np.float32(np.float32(np.float32(b) * w) * h))
+        k += 1
+    return ds, us, vs, k
+
+
 def simulation_run(d, u, v, events, nsteps, diff, visc, dt, kd=15, kp=20, smooth=True):
     """The reference's simulation driver around the GPU-semantics step: before step k
     the events of step k are added to zeroed source grids in order, source(i, j) +=
     value * width * height in float32 (src/simulation.cpp:44-51), then the step runs and
     the sources are cleared (src/simulation.cpp:53-64). events: (step, kind, i, j,
     value, value2), kind 0 = density, 1 = velocity."""
-    rows, cols = d.shape
-    w, h = np.float32(cols), np.float32(rows)
     d, u, v = (_c(a) for a in (d, u, v))
     k = 0
     for step in range(nsteps):
-        ds = np.zeros_like(d)
-        us = np.zeros_like(d)
-        vs = np.zeros_like(d)
-        while k < len(events) and events[k][0] == step:
-            _, kind, i, j, a, b = events[k]
-            if kind == 0:
-                ds[i, j] = np.float32(ds[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
-            else:
-                us[i, j] = np.float32(us[i, j] + np.float32(np.float32(np.float32(a) * w) * h))
-                vs[i, j] = np.float32(vs[i, j] + np.float32(np.float32(np.float32(b) * w) * h))
-            k += 1
+        ds, us, vs, k = script_sources(d.shape, events, k, step)
         d, u, v = gpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=kd, kp=kp, smooth=smooth)
     return d, u, v

@@ -8,6 +8,13 @@
   C shim ``oracle/ref_cpu_shim.cpp``. Built only where the checkout exists
   (``FLUID2D_REF_SRC``, default ``/root/reference/src``); it is used to generate
   and check the golden fixtures under ``tests/golden``.
+* ``oracle/_ref/ref_gpu.fatbin`` — the reference's unmodified GPU solver
+  (``src/fluid_solver_gpu.cu``) compiled for sm_103a as device code only. Built
+  where the checkout exists; device code does not depend on the host CPU, so the
+  file is usable on any GB300 host it is copied to.
+* ``oracle/_build/libref_gpu_runner.so`` — ``oracle/ref_gpu_runner.cpp`` (own
+  code), which loads that fatbinary with the CUDA driver API and drives the
+  reference's kernels in the reference's order. Built wherever CUDA is installed.
 """
 from __future__ import annotations
 
@@ -62,6 +69,45 @@ def build_ref(force: bool = False) -> pathlib.Path | None:
     return out
 
 
+REF_GPU_FATBIN = REF_OUT / "ref_gpu.fatbin"
+CUDA_HOME = pathlib.Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+
+
+def build_ref_gpu(force: bool = False) -> pathlib.Path | None:
+    """Compile the reference GPU solver's kernels where its sources are present."""
+    solver = REF_SRC / "fluid_solver_gpu.cu"
+    if not solver.exists():
+        return REF_GPU_FATBIN if REF_GPU_FATBIN.exists() else None
+    REF_OUT.mkdir(exist_ok=True)
+    if force or _stale(REF_GPU_FATBIN, [solver]):
+        tmp = REF_OUT / "ref_gpu.fatbin.tmp"
+        # Default nvcc flags (FMA contraction on), as the reference's CMake build compiles it;
+        # grid.hpp needs <cstddef> force-included.
+        _run([str(CUDA_HOME / "bin" / "nvcc"), "-std=c++14", "-fatbin", "-gencode", "arch=compute_103a,code=sm_103a",
+              "-include", "cstddef", f"-I{REF_SRC}", str(solver), "-o", str(tmp)])
+        os.replace(tmp, REF_GPU_FATBIN)
+    return REF_GPU_FATBIN
+
+
+def build_ref_gpu_runner(force: bool = False) -> pathlib.Path | None:
+    """The driver-API runner for that fatbinary (own code); None without a CUDA toolkit."""
+    hdr = CUDA_HOME / "include" / "cuda.h"
+    stubs = CUDA_HOME / "lib64" / "stubs"
+    if not hdr.exists():
+        return None
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "libref_gpu_runner.so"
+    src = HERE / "ref_gpu_runner.cpp"
+    if force or _stale(out, [src]):
+        tmp = out.with_suffix(".so.tmp")
+        _run(["g++", "-std=c++17", *COMMON, f"-I{CUDA_HOME / 'include'}", str(src), "-o", str(tmp),
+              f"-L{stubs}", "-lcuda"])
+        os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_gpu(force=True))
+    print(build_ref_gpu_runner(force=True))

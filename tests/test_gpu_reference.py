@@ -1,0 +1,127 @@
+"""CUDA path vs the reference's own GPU solver (GPU required).
+
+Two sources of the reference's outputs:
+  * the committed fixtures tests/golden/ref_gpu_*.npz (src/fluid_solver_gpu.cu compiled
+    unmodified for sm_103a and run on a GB300; tests/golden/make_golden_gpu.py);
+  * the reference's compiled kernels run live beside the CUDA path, where the prebuilt
+    fatbinary oracle/_ref/ref_gpu.fatbin is present (skipped otherwise).
+Tolerance: relative L-infinity per field per step, max|ours - ref| / max|ref| over all
+cells but the four corners (sampled rows and columns for the large fixtures, normalised
+by the full field's max), <= 1e-5. The reference's density splat adds with fp32 atomics
+in an unspecified order and its diffusion divides in FP64, which the CUDA path forms as
+a Newton-corrected FP32 quotient; everything else is the reference's arithmetic.
+"""
+import pathlib
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+SMALL = ["n3_random", "n5_random", "n34_sources", "n66_vortex", "n130_sources"]
+
+
+def _sampled_errors(f, step, fields):
+    ir, ic = f["idx_r"], f["idx_c"]
+    return [float(np.abs(x[np.ix_(ir, ic)].astype(np.float64) - f[f"s{step}_{nm}"]).max() /
+                  float(f[f"s{step}_{nm}_max"])) for nm, x in zip("duv", fields)]
+
+
+@pytest.mark.parametrize("case", SMALL)
+def test_matches_reference_fixture(fluid, case):
+    z = np.load(GOLDEN / f"ref_cpu_{case}.npz")
+    r = np.load(GOLDEN / f"ref_gpu_{case}.npz")
+    diff, visc, dt = (float(x) for x in z["params"])
+    kd, kp = (int(x) for x in r["iters"])
+    d, u, v = (np.array(z[k], np.float32) for k in ("d", "u", "v"))
+    rows, cols = d.shape
+    with fluid.Solver(rows, cols, diffuse_iterations=kd, pressure_iterations=kp, device=0) as s:
+        for _ in range(int(r["steps"])):
+            s.solve(d, z["ds"], diff, u, v, z["us"], z["vs"], visc, dt)
+    for got, key in ((d, "out_d"), (u, "out_u"), (v, "out_v")):
+        assert oracle.rel_linf(got, r[key]) <= TOL, key
+
+
+def test_matches_reference_app_configuration_100_steps(fluid):
+    """The reference app's own configuration (800x800, diffusion 0.5, viscosity 1e-6,
+    dt 0.02, src/app.cpp:8, 30-34) driven by its scripted drag through the
+    device-resident driver (fs_run_script, src/simulation.cpp:44-64), 100 steps,
+    compared at the fixture's checkpoints."""
+    f = np.load(GOLDEN / "ref_gpu_app800.npz")
+    n = int(f["n"])
+    diff, visc, dt = (float(x) for x in f["params"])
+    kd, kp = (int(x) for x in f["iters"])
+    events = [(int(a), int(b), int(c), int(d), float(e), float(g)) for a, b, c, d, e, g in f["events"]]
+    z = np.zeros((n, n), np.float32)
+    done = 0
+    with fluid.Solver(n, n, diffuse_iterations=kd, pressure_iterations=kp, device=0) as s:
+        s.upload(z, z, z)
+        s.upload_sources(z, z, z)
+        for cp in (int(c) for c in f["checkpoints"]):
+            seg = [(e[0] - done,) + e[1:] for e in events if done <= e[0] < cp]
+            s.run_script(seg, cp - done, diff, visc, dt)
+            done = cp
+            errs = _sampled_errors(f, cp, s.download())
+            assert max(errs) <= TOL, (cp, errs)
+
+
+@pytest.mark.parametrize("name", ["k15", "k40"])
+def test_matches_reference_at_2048(fluid, wl, name):
+    f = np.load(GOLDEN / f"ref_gpu_n2050_{name}.npz")
+    n = int(f["n"])
+    d, u, v = wl.portable_state(n, n, int(f["seed"]))
+    diff, visc, dt = (float(x) for x in f["params"])
+    kd, kp = (int(x) for x in f["iters"])
+    z = np.zeros_like(d)
+    with fluid.Solver(n, n, diffuse_iterations=kd, pressure_iterations=kp, device=0) as s:
+        s.upload(d, u, v)
+        s.upload_sources(z, z, z)
+        for step in (int(c) for c in f["checkpoints"]):
+            s.step(diff, visc, dt)
+            errs = _sampled_errors(f, step, s.download())
+            assert max(errs) <= TOL, (step, errs)
+
+
+@pytest.fixture(scope="module")
+def live_ref():
+    try:
+        R = oracle.ref_gpu_lib()
+    except RuntimeError as e:
+        pytest.skip(str(e))
+    if R is None:
+        pytest.skip("prebuilt reference fatbinary not present on this machine")
+    return R
+
+
+def test_benchmark_workload_vs_live_reference_20_steps(fluid, wl, live_ref):
+    """bench.py's workload (2048^2 vortex field, 40/40 sweeps, dt 0.05, rates 1e-5)
+    stepped side by side with the reference's own kernels for 20 steps."""
+    w = wl.vortex_field(2048, seed=2, kd=40, kp=40)
+    d, u, v = w.state()
+    rd, ru, rv = w.state()
+    worst = [0.0, 0.0, 0.0]
+    with fluid.Solver(w.rows, w.cols, diffuse_iterations=40, pressure_iterations=40, device=0) as s:
+        for _ in range(20):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            rd, ru, rv = oracle.ref_gpu_solve(rd, w.ds, w.diffusion, ru, rv, w.us, w.vs, w.viscosity, w.dt, kd=40,
+                                              kp=40)
+            for k, (g, r) in enumerate(((d, rd), (u, ru), (v, rv))):
+                worst[k] = max(worst[k], oracle.rel_linf(g, r))
+    assert max(worst) <= TOL, worst
+
+
+@pytest.mark.parametrize("n,kd,kp", [(130, 15, 20), (257, 15, 20), (1026, 30, 30)])
+def test_small_and_odd_grids_vs_live_reference(fluid, wl, live_ref, n, kd, kp):
+    w = wl.small_sources(n - 2, seed=n)
+    d, u, v = w.state()
+    rd, ru, rv = w.state()
+    with fluid.Solver(w.rows, w.cols, diffuse_iterations=kd, pressure_iterations=kp, device=0) as s:
+        for _ in range(10):
+            s.solve(d, w.ds, w.diffusion, u, v, w.us, w.vs, w.viscosity, w.dt)
+            rd, ru, rv = oracle.ref_gpu_solve(rd, w.ds, w.diffusion, ru, rv, w.us, w.vs, w.viscosity, w.dt, kd=kd,
+                                              kp=kp)
+            for g, r in ((d, rd), (u, ru), (v, rv)):
+                assert oracle.rel_linf(g, r) <= TOL
