@@ -89,7 +89,10 @@ def parse():
     return ap.parse_args()
 
 
-NCU_DRAM_BYTES_PER_CELL_PASS = 10.6
+# ncu on this build (profiles/stencil_kernel_2048_vortex.md): DRAM bytes read + written per
+# interior cell and field by one depth-8 pass at 2048^2, and the unit that bounds the pass
+NCU_DRAM_BYTES_PER_CELL_FIELD_PASS = 8.2
+NCU_BINDING = "SM instruction issue (ncu: issue active ~64 %, DRAM ~11 % of peak)"
 
 
 def dist_env():
@@ -310,7 +313,8 @@ def run_ours(a):
     cells = w.interior_cells
     value = cells * a.steps * world / (ms / 1e3)
 
-    # per-kernel CUDA-event profile of a few steps (stencil = dominant kind)
+    # per-kernel CUDA-event profile of steps in the timed graph's shape (same launches,
+    # same streams, the density branch beside the main stream); stencil = dominant kind
     stats0 = s.stats()
     prof = None
     for _ in range(a.profile_steps):
@@ -321,31 +325,44 @@ def run_ours(a):
             prof = p
         else:
             for k in prof:
-                for f in ("launches", "ms", "bytes"):
+                for f in prof[k]:
                     prof[k][f] += p[k][f]
     peak, peak_kind = measured_peak()
     st = prof["stencil"]
-    achieved = (st["bytes"] / st["launches"]) / (st["ms"] / st["launches"] / 1e3) / 1e9
-    # DRAM traffic per launch: ncu measured 10.6 B per interior cell per 8-sweep pass of
-    # this kernel (a 4096^2 pressure pass, dram__bytes_read + write); a launch moves
-    # (fields x cells) of them, so scale by the field-passes of a step over its launches
+    n_st = st["launches"]
+    ms_launch = st["ms"] / n_st
+    # achieved: the bytes each pass must move itself (every array it reads or writes,
+    # once) over its event time; the per-sweep model (every array once per sweep, the
+    # reference's one-kernel-per-sweep cost) is reported beside it
+    achieved = (st["pass_bytes"] / n_st) / (ms_launch / 1e3) / 1e9
+    model_gbps = (st["bytes"] / n_st) / (ms_launch / 1e3) / 1e9
     K = stats0["sweeps_per_pass"]
     diff_passes, proj_passes = -(-a.kd // K), -(-a.kp // K)
     field_passes = 3 * diff_passes + 2 * proj_passes
-    stencil_launches = diff_passes + 2 * proj_passes
-    traffic = NCU_DRAM_BYTES_PER_CELL_PASS * cells * field_passes / stencil_launches if K == 8 else None
-    step_ms_prof = sum(prof[k]["ms"] for k in prof) / a.profile_steps
-    shares = {k: round(prof[k]["ms"] / a.profile_steps / step_ms_prof, 4) for k in prof}
-    # every kernel kind against the same measured HBM peak (algorithmic bytes / event time)
-    per_kernel = {k: {"launches_per_step": prof[k]["launches"] / a.profile_steps,
-                      "ms_per_step": prof[k]["ms"] / a.profile_steps,
-                      "algorithmic_GBps": (prof[k]["bytes"] / (prof[k]["ms"] / 1e3) / 1e9) if prof[k]["ms"] > 0 else None}
-                  for k in prof if prof[k]["launches"]}
-    for v in per_kernel.values():
-        v["frac_of_hbm"] = v["algorithmic_GBps"] / peak if v["algorithmic_GBps"] else None
+    stencil_launches = 3 * diff_passes + 2 * proj_passes - diff_passes  # u and v share a launch
+    # DRAM traffic per launch: ncu's dram__bytes_read + write per field-pass of this kernel
+    # at 2048^2, depth 8 (profiles/stencil_kernel_2048_vortex.md), times the field-passes of
+    # an average launch of the step
+    traffic = (NCU_DRAM_BYTES_PER_CELL_FIELD_PASS * cells * field_passes / stencil_launches
+               if (K == 8 and a.size == 2048) else None)
+    main_ms = {k: (prof[k]["ms"] - prof[k]["branch_ms"]) / a.profile_steps for k in prof}
+    branch_ms = {k: prof[k]["branch_ms"] / a.profile_steps for k in prof}
+    # shares of all kernel time (both streams), comparable with ncu's serialised launch list
+    all_ms = sum(prof[k]["ms"] for k in prof)
+    shares = {k: round(prof[k]["ms"] / all_ms, 4) for k in prof}
+    per_kernel = {}
+    for k in prof:
+        if not prof[k]["launches"]:
+            continue
+        ms_k = prof[k]["ms"]
+        gbps = (prof[k]["pass_bytes"] / (ms_k / 1e3) / 1e9) if ms_k > 0 else None
+        per_kernel[k] = {"launches_per_step": prof[k]["launches"] / a.profile_steps,
+                         "branch_launches_per_step": prof[k]["branch_launches"] / a.profile_steps,
+                         "ms_per_step_main_stream": main_ms[k], "ms_per_step_branch": branch_ms[k],
+                         "pass_GBps": gbps, "frac_of_hbm": gbps / peak if gbps else None}
 
     # end to end through the reference-shaped call with pinned host buffers
-    e2e = None
+    e2e = e2e_pageable = None
     if not a.no_e2e:
         pins = [pkg.PinnedArray(w.rows, w.cols) for _ in range(6)]
         for p_, src in zip(pins, (w.d, w.ds, w.u, w.v, w.us, w.vs)):
@@ -366,9 +383,28 @@ def run_ours(a):
             el = float(t.item())
         fb = w.rows * w.cols * 4
         e2e = {"value": cells * e2e_steps * world / el, "unit": "cell-steps/s", "h2d_bytes_per_step": 6 * fb,
-               "d2h_bytes_per_step": 3 * fb, "steps": e2e_steps, "ms_per_step": 1e3 * el / e2e_steps}
+               "d2h_bytes_per_step": 3 * fb, "steps": e2e_steps, "ms_per_step": 1e3 * el / e2e_steps,
+               "host_memory": "pinned (fs_host_alloc)"}
         for p_ in pins:
             p_.free()
+        # the same call on pageable host memory, which is what the C++ drop-in adapter
+        # passes (the reference's grid<float> is a std::vector)
+        pg = [np.array(x, np.float32, copy=True) for x in (w.d, w.ds, w.u, w.v, w.us, w.vs)]
+        for _ in range(2):
+            s.solve(pg[0], pg[1], w.diffusion, pg[2], pg[3], pg[4], pg[5], w.viscosity, w.dt)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.solve(pg[0], pg[1], w.diffusion, pg[2], pg[3], pg[4], pg[5], w.viscosity, w.dt)
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        e2e_pageable = {"value": cells * e2e_steps * world / el, "unit": "cell-steps/s",
+                        "h2d_bytes_per_step": 6 * fb, "d2h_bytes_per_step": 3 * fb, "steps": e2e_steps,
+                        "ms_per_step": 1e3 * el / e2e_steps, "host_memory": "pageable (numpy)"}
 
     if e2e:
         # the host call's own step (uploads overlapped with a split diffusion on large grids)
@@ -384,17 +420,26 @@ def run_ours(a):
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                             "traffic_source": "ncu dram bytes of a 4096^2 8-sweep pass (10.6 B/cell), scaled "
-                                               "to this launch's cells",
-                             "kernel": "stencil_kernel", "launches_profiled": st["launches"],
-                             "algorithmic_bytes_per_launch": st["bytes"] / st["launches"],
-                             "ms_per_launch": st["ms"] / st["launches"]},
+                             "kernel": "stencil_kernel", "launches_profiled": n_st,
+                             "bytes_per_launch": st["pass_bytes"] / n_st,
+                             "bytes_model": "each array a pass reads or writes, once (12 B per interior cell "
+                                            "and field for a middle pass, 16 first, 24 last pressure)",
+                             "ms_per_launch": ms_launch,
+                             "traffic_source": "ncu dram__bytes_read+write per field-pass at 2048^2, depth 8 "
+                                               f"({NCU_DRAM_BYTES_PER_CELL_FIELD_PASS} B per cell), "
+                                               "profiles/stencil_kernel_2048_vortex.md",
+                             "model_equivalent_GBps": model_gbps, "model_equivalent_frac": model_gbps / peak,
+                             "model": "per-sweep model, 12 B per cell and field per sweep (the reference's "
+                                      "one-kernel-per-sweep traffic)",
+                             "binding_resource": NCU_BINDING},
                 "kernel_shares": shares,
                 "kernels": per_kernel,
+                "stencil_ms_per_step_main_stream": main_ms["stencil"],
                 "step_algorithmic_bytes_per_cell": sum(prof[k]["bytes"] for k in prof) / a.profile_steps / cells,
                 "clocks": clk, "wall_s": t_wall}
         if e2e:
             line["e2e"] = e2e
+            line["e2e_pageable"] = e2e_pageable
         if not a.no_cpu and world == 1:
             line["cpu_baseline"] = cpu_baseline(w, a.kd, a.kp)
         print(json.dumps(line), flush=True)
@@ -556,71 +601,105 @@ def run_gauss_seidel(a):
 
 def run_batch(a):
     """256 independent grids, N uniform in {64..1024}, 30/30 sweeps: one fs_batch
-    (one launch per sub-step, graph per step) vs the same grids as 256 handles."""
+    (one launch per sub-step, graph per step) vs the same grids as 256 handles. Under
+    torchrun (N > 1) the grids are dealt to ranks by longest-processing-time-first on
+    cells x sweeps (replicas.shard), each rank steps its own batch, and the ranks meet
+    only at the barriers around the timed region; the value is all ranks' cells over the
+    slowest rank's time."""
     import torch
 
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if world > 1 else 0
     pkg = __graft_entry__.load_package()
-    from fluid2d_gb300 import build_lib, workloads
+    from fluid2d_gb300 import build_lib, replicas, workloads
 
     build_lib.build()
     kd = kp = 30
-    sims = workloads.batch(a.count, seed=4, kd=kd, kp=kp)
+    all_sims = workloads.batch(a.count, seed=4, kd=kd, kp=kp)
+    mine = replicas.shard([(w.rows, w.cols) for w in all_sims], world, rank, kd, kp)
+    sims = [all_sims[i] for i in mine]
     shapes = [(w.rows, w.cols) for w in sims]
     cells = sum(w.interior_cells for w in sims)
+    total_cells = sum(w.interior_cells for w in all_sims)
     w0 = sims[0]
-    cfg = dict(diffuse_iterations=kd, pressure_iterations=kp, device=0, check_finite=0)
+    cfg = dict(diffuse_iterations=kd, pressure_iterations=kp, device=dev, check_finite=0)
     if a.sweeps:
         cfg["sweeps_per_pass"] = a.sweeps
     if a.tile_rows:
         cfg["tile_rows"] = a.tile_rows
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     b = pkg.Batch(shapes, **cfg)
     for k, w in enumerate(sims):
         b.upload(k, *w.state())
         b.upload_sources(k, *w.sources())
-    stream = torch.cuda.ExternalStream(b.stream, device=0)
+    stream = torch.cuda.ExternalStream(b.stream, device=dev)
 
     def flush_l2():
         with torch.cuda.stream(stream):
             flush.zero_()
 
-    b.step(w0.diffusion, w0.viscosity, w0.dt, nsteps=a.warmup)
+    b.step(w0.diffusion, w0.viscosity, w0.dt, nsteps=max(3, a.warmup))
     l0 = b.stats()["kernel_launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
     ms_b = _timed_steps(lambda: b.step(w0.diffusion, w0.viscosity, w0.dt, 1, sync=False), b.sync, stream, a.steps,
-                        flush_l2, torch, 0)
+                        flush_l2, torch, dev)
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+        t = torch.tensor([ms_b], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_b = float(t.item())
     launches = b.stats()["kernel_launches"] - l0
     st = b.stats()
     b.close()
-    # the same grids as independent handles, stepped one after another per step
-    hs = []
-    for w in sims:
-        s = pkg.Solver(w.rows, w.cols, **cfg)
-        s.upload(*w.state())
-        s.upload_sources(*w.sources())
-        s.step(w.diffusion, w.viscosity, w.dt, nsteps=1)
-        hs.append(s)
-    streams = [torch.cuda.ExternalStream(h.device_view().stream, device=0) for h in hs]
-    steps_l = max(2, a.steps // 4)
-    torch.cuda.synchronize(0)
-    t0 = time.perf_counter()
-    for _ in range(steps_l):
+    looped = None
+    if world == 1:
+        # the same grids as independent handles, stepped one after another per step
+        hs = []
+        for w in sims:
+            s = pkg.Solver(w.rows, w.cols, **cfg)
+            s.upload(*w.state())
+            s.upload_sources(*w.sources())
+            s.step(w.diffusion, w.viscosity, w.dt, nsteps=1)
+            hs.append(s)
+        steps_l = max(2, a.steps // 4)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(steps_l):
+            for h in hs:
+                h.step(w0.diffusion, w0.viscosity, w0.dt, 1, sync=False)
+            for h in hs:
+                h.sync()
+        ms_l = (time.perf_counter() - t0) * 1e3
         for h in hs:
-            h.step(w0.diffusion, w0.viscosity, w0.dt, 1, sync=False)
-        for h in hs:
-            h.sync()
-    ms_l = (time.perf_counter() - t0) * 1e3
-    for h in hs:
-        h.close()
-    line = {"metric": metric_name(), "value": cells * a.steps / (ms_b / 1e3), "unit": "cell-steps/s", "n_gpus": 1,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_b / a.steps, "higher_is_better": True,
-            "dtype": "f32", "data": "synthetic (seeded vortex fields + sources)", "gpu_launches": launches,
-            "config": {"workload": f"batch of {len(sims)} grids, N uniform in 64..1024, Kd=Kp=30, dt 0.05",
-                       "interior_cells": cells, "launches_per_step": st["launches_per_step"],
-                       "sweeps_per_pass": st["sweeps_per_pass"], "tile_rows": st["tile_rows"],
-                       "l2": "flushed between timed steps"},
-            "looped_handles": {"value": cells * steps_l / (ms_l / 1e3), "ms_per_step": ms_l / steps_l,
-                               "timing": "host wall clock, one graph per handle per step"}}
-    print(json.dumps(line), flush=True)
+            h.close()
+        looped = {"value": cells * steps_l / (ms_l / 1e3), "ms_per_step": ms_l / steps_l,
+                  "timing": "host wall clock, one graph per handle per step"}
+    if rank == 0:
+        line = {"metric": metric_name(), "value": total_cells * a.steps / (ms_b / 1e3), "unit": "cell-steps/s",
+                "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_b / a.steps,
+                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded vortex fields + sources)", "gpu_launches": launches,
+                "config": {"workload": f"batch of {len(all_sims)} grids, N uniform in 64..1024, Kd=Kp=30, dt 0.05",
+                           "interior_cells": total_cells, "rank0_grids": len(sims),
+                           "launches_per_step": st["launches_per_step"], "sweeps_per_pass": st["sweeps_per_pass"],
+                           "tile_rows": st["tile_rows"], "l2": "flushed between timed steps",
+                           "parallelism": f"grids dealt to {world} rank(s) by LPT on cells x sweeps"},
+                "clocks": clk}
+        if looped:
+            line["looped_handles"] = looped
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
 
 
 def run_residual(a):

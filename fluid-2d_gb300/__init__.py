@@ -59,7 +59,8 @@ KIND_NAMES = ("stencil", "splat", "finish", "advect", "memset")
 
 class fs_kernel_times(C.Structure):
     _fields_ = [("launches", C.c_int * FS_NUM_KINDS), ("ms", C.c_double * FS_NUM_KINDS),
-                ("algorithmic_bytes", C.c_double * FS_NUM_KINDS)]
+                ("algorithmic_bytes", C.c_double * FS_NUM_KINDS), ("pass_bytes", C.c_double * FS_NUM_KINDS),
+                ("branch_launches", C.c_int * FS_NUM_KINDS), ("branch_ms", C.c_double * FS_NUM_KINDS)]
 
 
 class fs_device_view(C.Structure):
@@ -296,11 +297,14 @@ class Solver:
                 "learned_used": st.learned_used, "learned_fallback": st.learned_fallback}
 
     def profile_step(self, diffusion_rate, viscosity, dt) -> dict:
-        """One eager step with CUDA events around every launch; per kernel kind:
-        launches, milliseconds and algorithmic bytes."""
+        """One eager step in the graph's shape with CUDA events around every launch on its
+        own stream; per kernel kind: launches, milliseconds, per-sweep-model bytes, pass
+        bytes, and the launches / milliseconds that ran on the concurrent density branch."""
         t = fs_kernel_times()
         _check(self._lib.fs_profile_step(self._h, diffusion_rate, viscosity, dt, C.byref(t)))
-        return {KIND_NAMES[k]: {"launches": t.launches[k], "ms": t.ms[k], "bytes": t.algorithmic_bytes[k]}
+        return {KIND_NAMES[k]: {"launches": t.launches[k], "ms": t.ms[k], "bytes": t.algorithmic_bytes[k],
+                                "pass_bytes": t.pass_bytes[k], "branch_launches": t.branch_launches[k],
+                                "branch_ms": t.branch_ms[k]}
                 for k in range(FS_NUM_KINDS)}
 
     def render_density(self, multipliers=(1.0, 1.0, 1.0)) -> np.ndarray:

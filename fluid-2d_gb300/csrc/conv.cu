@@ -158,24 +158,35 @@ __global__ void __launch_bounds__(128) conv3x3_tc_kernel(const ConvArgs P) {
         }
         tc::commit_to(bar);
     }
-    // bounded wait for the MMAs
-    uint32_t spins = 0;
-    while (!tc::mbar_try_wait(bar, 0)) {
-        if (++spins > kWaitLimit) {
-            if (P.err) atomicOr(P.err, 1);
-            break;
-        }
-    }
+    // Bounded wait for the MMAs. Tensor memory is read and freed only after the commit
+    // has arrived, since an MMA still in flight writes it (and reads the shared-memory
+    // operands). If the first bound runs out the CTA flags the error, skips the
+    // epilogue, and waits once more with the same bound before freeing; a CTA whose
+    // warp 0 never sees the arrival leaves the allocation in place rather than free
+    // columns an MMA may still write (the host treats the flagged error as fatal for
+    // the network).
+    auto wait_commit = [&]() {
+        uint32_t spins = 0;
+        while (!tc::mbar_try_wait(bar, 0))
+            if (++spins > kWaitLimit) return false;
+        return true;
+    };
+    bool arrived = wait_commit();
+    if (!arrived && P.err) atomicOr(P.err, 1);
     tc::fence_after_sync();
-
-    float v[32];
-    tc::tmem_ld_32x32(taddr + ((uint32_t)(warp * 32) << 16), v);
-    const long p = p0 + warp * 32 + lane;
-    if (p < npix) epilogue_store(P, p, v);
+    if (__all_sync(0xffffffffu, arrived)) {
+        float v[32];
+        tc::tmem_ld_32x32(taddr + ((uint32_t)(warp * 32) << 16), v);
+        const long p = p0 + warp * 32 + lane;
+        if (p < npix) epilogue_store(P, p, v);
+    } else {
+        arrived = wait_commit();
+    }
+    const bool free_ok = __all_sync(0xffffffffu, arrived);
 
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(taddr, 32);
+    if (warp == 0 && free_ok) tc::tmem_dealloc(taddr, 32);
 }
 
 // Reference: one thread per (pixel, output channel), FP32 accumulation of BF16 values.

@@ -78,6 +78,15 @@ enum FieldId { F_D = 0, F_U = 1, F_V = 2 };
 // Lets other translation units of the library report through fs_last_error().
 int fs::record_error(int code, const char* msg) { return fail(code, msg); }
 
+// A launch of a profiled step: its kind, algorithmic bytes, and whether it ran on the
+// density side branch (concurrently with the main stream).
+struct ProfMark {
+    int kind;
+    double bytes;       // per-sweep model: every input read and output written once per sweep
+    double pass_bytes;  // the arrays the launch itself must read and write once
+    bool branch;
+};
+
 struct fs_solver {
     fs_config cfg{};
     int device = 0;
@@ -133,6 +142,7 @@ struct fs_solver {
     fs_source_event* d_events = nullptr;  // device copy of a source script
     int d_events_cap = 0;
     bool net_ready = false;
+    long long steps_reported = -1;  // stats.steps when check_flags last reported the residual solves
     cudaStream_t stream = nullptr;
     // density advection runs on `side` beside the first projection (a parallel branch of
     // the step graph), forked and joined by side_ev
@@ -157,7 +167,7 @@ struct fs_solver {
     // per-kernel event timing (fs_profile_step); null outside a profiled step
     fs_kernel_times* prof = nullptr;
     std::vector<cudaEvent_t> prof_events;
-    std::vector<std::pair<int, double>> prof_marks;  // (kind, algorithmic bytes) per launch
+    std::vector<ProfMark> prof_marks;  // one per profiled launch
 };
 
 namespace {
@@ -268,37 +278,41 @@ struct Counter {
 
 double interior_cells(const fs_solver* s) { return (double)(s->rows - 2) * (double)(s->cols - 2); }
 
-// Event before a launch (profiled steps only).
-int prof_begin(fs_solver* s) {
+// Event before a launch on stream st (profiled steps only).
+int prof_begin(fs_solver* s, cudaStream_t st) {
     if (!s->prof) return FS_OK;
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     s->prof_events.push_back(e);
-    CK(cudaEventRecord(e, s->stream));
+    CK(cudaEventRecord(e, st));
     return FS_OK;
 }
 
-// Event after a launch, tagged with its kind and algorithmic bytes.
-int prof_end(fs_solver* s, int kind, double bytes) {
+// Event after a launch on stream st, tagged with its kind, its algorithmic bytes and
+// whether it ran on the density side branch (concurrently with the main stream).
+int prof_end(fs_solver* s, cudaStream_t st, int kind, double bytes, double pass_bytes) {
     if (!s->prof) return FS_OK;
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     s->prof_events.push_back(e);
-    CK(cudaEventRecord(e, s->stream));
-    s->prof_marks.push_back({kind, bytes});
+    CK(cudaEventRecord(e, st));
+    s->prof_marks.push_back({kind, bytes, pass_bytes, st != s->stream});
     return FS_OK;
 }
 
-#define PROF_BEGIN(s)                                 \
+#define PROF_BEGIN_ON(s, st)                          \
     do {                                              \
-        int rc_ = prof_begin(s);                      \
+        int rc_ = prof_begin(s, st);                  \
         if (rc_ != FS_OK) return rc_;                 \
     } while (0)
-#define PROF_END(s, kind, bytes)                      \
-    do {                                              \
-        int rc_ = prof_end(s, kind, bytes);           \
-        if (rc_ != FS_OK) return rc_;                 \
+#define PROF_END_PASS(s, st, kind, bytes, pass_bytes)        \
+    do {                                                     \
+        int rc_ = prof_end(s, st, kind, bytes, pass_bytes);  \
+        if (rc_ != FS_OK) return rc_;                        \
     } while (0)
+#define PROF_END_ON(s, st, kind, bytes) PROF_END_PASS(s, st, kind, bytes, bytes)
+#define PROF_BEGIN(s) PROF_BEGIN_ON(s, (s)->stream)
+#define PROF_END(s, kind, bytes) PROF_END_ON(s, (s)->stream, kind, bytes)
 
 // Diffusion of a subset of {d, u, v}: add_sources fused into pass 0. Returns the
 // buffer holding each field's result in out[].
@@ -337,11 +351,13 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
             begin += f.tiles_x * f.tiles_y;
             cur[q] = dst;
         }
-        // per field: 12 B/cell per sweep (read x and x0, write x) + 12 B/cell add_sources
+        // per field: 12 B/cell per sweep (read x and x0, write x) + 12 B/cell add_sources;
+        // the pass itself reads x and x0 (first: x and s) and writes x (first: and x0)
         const double bytes = nf * interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0));
-        PROF_BEGIN(s);
+        const double pass_bytes = nf * interior_cells(s) * (pass == 0 ? 16.0 : 12.0);
+        PROF_BEGIN_ON(s, st);
         CK(launch_stencil(L, s->tile_rows, st));
-        PROF_END(s, FS_KIND_STENCIL, bytes);
+        PROF_END_PASS(s, st, FS_KIND_STENCIL, bytes, pass_bytes);
         cnt.launches++;
         cnt.passes++;
     }
@@ -699,12 +715,16 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
             f.v_out = v_out;
             f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
         }
-        // 12 B/cell per sweep (read p and div, write p), + 12 divergence, + 20 gradient
+        // 12 B/cell per sweep (read p and div, write p), + 12 divergence, + 20 gradient;
+        // the pass itself reads p and div (first: u and v, and p when warm) and writes p
+        // (first: and div; last: u and v instead of p)
         const double bytes =
             interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0) + (last ? 20.0 : 0.0));
+        const double pass_bytes =
+            interior_cells(s) * ((pass == 0 ? 8.0 + (pin ? 4.0 : 0.0) + 4.0 : 8.0) + (last ? 16.0 : 4.0));
         PROF_BEGIN(s);
         CK(launch_stencil(L, s->tile_rows, s->stream));
-        PROF_END(s, FS_KIND_STENCIL, bytes);
+        PROF_END_PASS(s, s->stream, FS_KIND_STENCIL, bytes, pass_bytes);
         cnt.launches++;
         cnt.passes++;
         if (pass == 0 && (rc = capture_div(s, slot)) != FS_OK) return rc;
@@ -719,15 +739,15 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
 int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const float* u, const float* v, float dt,
                            Counter& cnt, cudaStream_t st) {
     const AdvectArgs A = advect_args(s, dt);
-    PROF_BEGIN(s);
+    PROF_BEGIN_ON(s, st);
     CK(cudaMemsetAsync(s->acc, 0, s->field_floats * sizeof(float), st));
-    PROF_END(s, FS_KIND_MEMSET, 0.0);
-    PROF_BEGIN(s);
+    PROF_END_ON(s, st, FS_KIND_MEMSET, 0.0);
+    PROF_BEGIN_ON(s, st);
     CK(launch_splat(d0, u, v, s->acc, A, st));
-    PROF_END(s, FS_KIND_SPLAT, 16.0 * interior_cells(s));  // read d0, u, v; write d
-    PROF_BEGIN(s);
+    PROF_END_ON(s, st, FS_KIND_SPLAT, 16.0 * interior_cells(s));  // read d0, u, v; write d
+    PROF_BEGIN_ON(s, st);
     CK(launch_density_finish(s->acc, d_out, s->cfg.smooth, A, s->cfg.check_finite ? s->flags : nullptr, st));
-    PROF_END(s, FS_KIND_FINISH, 8.0 * interior_cells(s));  // smooth: read d, write d
+    PROF_END_ON(s, st, FS_KIND_FINISH, 8.0 * interior_cells(s));  // smooth: read d, write d
     cnt.launches += 2;
     return FS_OK;
 }
@@ -735,16 +755,13 @@ int enqueue_advect_density(fs_solver* s, const float* d0, float* d_out, const fl
 // The density half of a step: forward advection of the diffused density by the step's
 // initial velocity (still in the state), then smoothing — and, with diffuse = true, the
 // density diffusion before it. It depends on nothing the velocity half writes before its
-// second projection, so outside profiled steps it runs on the side stream, beside the
-// velocity diffusion and the first projection, and join_density() brings it back before
-// the state velocity is rewritten. dif_d: the diffused density when diffuse = false.
+// second projection, so it runs on the side stream, beside the velocity diffusion and
+// the first projection, and join_density() brings it back before the state velocity is
+// rewritten. dif_d: the diffused density when diffuse = false.
 int fork_density(fs_solver* s, const float* dif_d, float diff, float dt, bool diffuse, Counter& cnt) {
-    cudaStream_t st = s->stream;
-    if (!s->prof) {
-        CK(cudaEventRecord(s->side_ev[0], s->stream));
-        CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
-        st = s->side;
-    }
+    CK(cudaEventRecord(s->side_ev[0], s->stream));
+    CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
+    cudaStream_t st = s->side;
     int rc;
     if (diffuse) {
         const int fd = F_D;
@@ -753,12 +770,12 @@ int fork_density(fs_solver* s, const float* dif_d, float diff, float dt, bool di
         dif_d = out;
     }
     if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, st)) != FS_OK) return rc;
-    if (!s->prof) CK(cudaEventRecord(s->side_ev[1], s->side));
+    CK(cudaEventRecord(s->side_ev[1], s->side));
     return FS_OK;
 }
 
 int join_density(fs_solver* s) {
-    if (!s->prof) CK(cudaStreamWaitEvent(s->stream, s->side_ev[1], 0));
+    CK(cudaStreamWaitEvent(s->stream, s->side_ev[1], 0));
     return FS_OK;
 }
 
@@ -796,9 +813,8 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
         cnt.launches += 4;
         return FS_OK;
     }
-    if (s->prof || !s->density_branch) {
-        // one diffusion launch per pass serves all three fields (and profiled steps run
-        // sequentially)
+    if (!s->density_branch) {
+        // one diffusion launch per pass serves all three fields
         const int fields[3] = {F_D, F_U, F_V};
         const float rates[3] = {diff, visc, visc};
         float* dif[3];
@@ -897,7 +913,24 @@ int check_flags(fs_solver* s) {
             return fail(FS_ERR_NONFINITE, "the step produced a non-finite value");
         }
     }
-    if (s->cfg.pressure_tolerance > 0.f && s->stats.steps > 0) {
+    if (s->net_ready && s->net.err) {
+        // a tensor-core wait of the network's convolutions gave up (conv3x3_tc_kernel):
+        // stop using the network until fs_set_network loads it again
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, s->net.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (h) {
+            CK(cudaMemsetAsync(s->net.err, 0, sizeof(int), s->stream));
+            s->net_ready = false;
+            destroy_graph(s);
+            return fail(FS_ERR_TIMEOUT, "learned correction: a tensor-core wait gave up; the network is disabled "
+                                        "until fs_set_network");
+        }
+    }
+    // the residual solves' outcome is reported once per step: later syncs without a new
+    // step do not report it again
+    if (s->cfg.pressure_tolerance > 0.f && s->stats.steps > 0 && s->steps_reported != s->stats.steps) {
+        s->steps_reported = s->stats.steps;
         SolveCtrl c[2];
         int rc = read_solve_ctrl(s, c);
         if (rc != FS_OK) return rc;
@@ -1535,15 +1568,21 @@ int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float d
     int rc = enqueue_step(s, diffusion_rate, viscosity, dt, cnt);
     s->prof = nullptr;
     cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->side);
     if (rc == FS_OK && e != cudaSuccess) rc = cuda_fail(e, "fs_profile_step: sync");
     if (rc == FS_OK) {
         for (size_t k = 0; k < s->prof_marks.size() && 2 * k + 1 < s->prof_events.size(); ++k) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, s->prof_events[2 * k], s->prof_events[2 * k + 1]);
-            const int kind = s->prof_marks[k].first;
-            out->launches[kind] += 1;
-            out->ms[kind] += ms;
-            out->algorithmic_bytes[kind] += s->prof_marks[k].second;
+            const ProfMark& m = s->prof_marks[k];
+            out->launches[m.kind] += 1;
+            out->ms[m.kind] += ms;
+            out->algorithmic_bytes[m.kind] += m.bytes;
+            out->pass_bytes[m.kind] += m.pass_bytes;
+            if (m.branch) {
+                out->branch_launches[m.kind] += 1;
+                out->branch_ms[m.kind] += ms;
+            }
         }
         s->stats.kernel_launches += cnt.launches;
         s->stats.steps++;

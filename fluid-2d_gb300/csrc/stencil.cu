@@ -38,118 +38,212 @@
 namespace fs {
 namespace {
 
-__device__ __forceinline__ float diffuse_update(float x0, float L, float R, float U, float D, float a,
-                                                float dh, float dl, float rf) {
-    // (x0 + a*(L + R + U + D)) / (1 + 4a), fluid_solver_gpu.cu:81-82; the compiled
-    // reference fuses x0 + a*sum into one FMA
-    float s = __fadd_rn(L, R);
-    s = __fadd_rn(s, U);
-    s = __fadd_rn(s, D);
-    const float num = __fmaf_rn(a, s, x0);
-    float q = __fmul_rn(num, rf);
-    float e = __fmaf_rn(-q, dh, num);
-    e = __fmaf_rn(-q, dl, e);
-    return __fmaf_rn(e, rf, q);
-}
-
-__device__ __forceinline__ float pressure_update(float dv, float L, float R, float U, float D) {
-    // (div + R + L + D + U) / 4, fluid_solver_gpu.cu:187-188
-    float s = __fadd_rn(dv, R);
-    s = __fadd_rn(s, L);
-    s = __fadd_rn(s, D);
-    s = __fadd_rn(s, U);
-    return __fmul_rn(s, 0.25f);
-}
-
-// All sweeps of one tile, register-blocked. The region's RH x 128 cells are split
-// among the CTA's NW warps: warp w owns rows [w*SRB, w*SRB + SRB), and lane l of a
-// warp owns the four columns 4l .. 4l+3 of those rows, so each thread holds a
-// SRB x 4 block of the field (x) in registers for the whole pass; the constant term
-// (x0 or div) stays in shared memory at koff and is read as one float4 per row. Per
-// sweep and row, the left neighbour of column 0 and the right neighbour of column 3
-// come from the adjacent lanes by warp shuffles, and the rows above and below the block
-// from the adjacent warps through a small double-buffered exchange area at eoff (two
-// rows per warp, written and read as float4); everything else is in the thread's own
-// registers. Per 128 cell updates of a warp that is 2 shuffles, 4 wavefronts of
-// constant loads and 4 * 4 / SRB wavefronts of row exchange, against 16 wavefronts of
-// shared loads and stores for a one-column-per-thread rolling window (three loads and
-// one store per update). One barrier per sweep.
+// ---------------------------------------------------------------------------
+// Register-blocked sweeps.
+//
+// The region's RH x 128 cells are split among the CTA's NW warps: warp w owns rows
+// [8w, 8w + 8) and lane l of a warp owns the four columns 4l .. 4l+3 of those rows, so
+// each thread holds an 8 x 4 block of the field in registers for the whole pass, as
+// float2 row pairs P[j][q] = (row j, row j + 4) of column q (j = 0..3). One packed
+// FP32 instruction (FADD2 / FMUL2 / FFMA2, each lane rounding exactly as the scalar
+// form) then updates two cells. Per sweep and row pair:
+//   left / right neighbours: the thread's own columns, except the left one of column 0
+//     and the right one of column 3, which come from the adjacent lanes by shuffles;
+//   up / down neighbours: the thread's own rows, except above row 0 and below row 7,
+//     which come from the adjacent warps through a small double-buffered exchange area
+//     in shared memory (each warp publishes its rows 0 and 7 as float4);
+//   constant term (x0 or div): shared memory, in a layout where one float4 holds the
+//     row pair's values of two columns (kidx).
+// The new values go to a second register block (the sweep loop alternates the two), so
+// no register is copied. Per 128 cell updates of a warp: 8 FP instructions per cell pair
+// (diffusion) or 5 (pressure), 2 shuffles, 4 wavefronts of constant loads and 4 of row
+// exchange, and one barrier per sweep.
 // Cells at the region border read clamped or wrapped neighbours and compute values that
 // nothing stored depends on (the halo is at least the number of sweeps).
-//   EDGE = false: the region lies inside the domain interior; every cell updates.
-//   EDGE = true:  only interior cells update (row_int / col_int bits), the others keep
-//                 their value. The reference fills the domain-edge cells after every
-//                 sweep with their inner neighbour's new value times a sign
-//                 (set_boundary_*, fluid_solver_gpu.cu:11-54), and the only cells that
-//                 read an edge cell are those inner neighbours. So from the second sweep
-//                 on, an interior cell next to an edge reads sign * (its own current
-//                 value) in place of the edge cell, the same float the fill would have
-//                 stored there, and the edge cells themselves are filled once, after the
-//                 last sweep (fill_edges). The first sweep reads the edge cells as
-//                 loaded. i1 / i2: block row of grid row 1 / rows - 2 (or out of range);
-//                 q1 / q2: block column of grid column 1 / cols - 2 (or out of range).
-template <bool DIFF, bool EDGE, int NW, int SRB>
-__device__ __forceinline__ void run_sweeps(float (&x)[SRB][4], int koff, int eoff, int nsweeps, int w, int lane, unsigned row_int, unsigned col_int, int i1,
-                                           int i2, int q1, int q2, float s_lr, float s_tb, float a, float dh, float dl,
-                                           float rf) {
+//
+// Domain edges. The reference fills the edge cells after every sweep with their inner
+// neighbour's new value times a sign (set_boundary_*, fluid_solver_gpu.cu:11-54), corners
+// excepted. Here every cell of the block is updated by the stencil (edge, corner and
+// outside cells compute values nothing uses), and from the second sweep on, before the
+// sweep reads them, the edge cells the interior reads are filled exactly as the
+// reference fills them: in the thread itself where edge and inner cell share a thread,
+// and otherwise in the value received from the neighbour (the shuffled column or the
+// exchanged row is replaced by sign x the interior cell's own value, the float the fill
+// would have stored there). After the last sweep fill_edges applies the fill for the
+// stores, and the corners get their loaded values back (restore_corners).
+
+struct Coef2 {
+    float2 a, ndh, ndl, rf;  // diffusion: a, -dh, -dl and rf of the quotient (head of this file)
+};
+
+template <bool DIFF>
+__device__ __forceinline__ float2 update2(float2 k, float2 L, float2 R, float2 U, float2 D, const Coef2& c) {
+    if (DIFF) {
+        // (x0 + a*(L + R + U + D)) / (1 + 4a), fluid_solver_gpu.cu:81-82: the numerator
+        // fused as in the compiled reference, the quotient Newton-corrected in FP32 (see
+        // the head of this file)
+        float2 s = __fadd2_rn(L, R);
+        s = __fadd2_rn(s, U);
+        s = __fadd2_rn(s, D);
+        const float2 num = __ffma2_rn(c.a, s, k);
+        const float2 q = __fmul2_rn(num, c.rf);
+        float2 e = __ffma2_rn(q, c.ndh, num);
+        e = __ffma2_rn(q, c.ndl, e);
+        return __ffma2_rn(e, c.rf, q);
+    } else {
+        // (div + R + L + D + U) / 4, fluid_solver_gpu.cu:187-188
+        float2 s = __fadd2_rn(k, R);
+        s = __fadd2_rn(s, L);
+        s = __fadd2_rn(s, D);
+        s = __fadd2_rn(s, U);
+        return __fmul2_rn(s, make_float2(0.25f, 0.25f));
+    }
+}
+
+// Offset of the constant term of region cell (r, c) in its shared buffer: per warp
+// block of 8 rows, row pair j = r & 3, plane (c & 2) (columns 0-1 or 2-3 of a lane),
+// lane c / 4, then (column c & 1, row half (r >> 2) & 1) — so that a lane's float4 at
+// (j, plane) is (k[j][q], k[j+4][q], k[j][q+1], k[j+4][q+1]) and a warp's float4 loads
+// of one plane are 512 contiguous bytes.
+__device__ __forceinline__ int kidx(int r, int c) {
+    return (r >> 3) * (8 * kRegionW) + (r & 3) * (2 * kRegionW) + ((c >> 1) & 1) * kRegionW + (c >> 2) * 4 +
+           (c & 1) * 2 + ((r >> 2) & 1);
+}
+
+struct EdgeGeom {
+    int i1, i2;  // block row of grid row 1 / rows - 2 (out of 0..7: none)
+    int q1, q2;  // block column of grid column 1 / cols - 2 (out of 0..3: none)
+    float s_lr, s_tb;
+};
+
+template <int I> __device__ __forceinline__ float& rowref(float2 (&X)[4][4], int q) {
+    return (I >> 2) ? X[I & 3][q].y : X[I & 3][q].x;
+}
+template <int DST, int SRC> __device__ __forceinline__ void fill_row(float2 (&X)[4][4], float sg) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rowref<DST>(X, q) = __fmul_rn(sg, rowref<SRC>(X, q));
+}
+template <int DST, int SRC> __device__ __forceinline__ void fill_col(float2 (&X)[4][4], float sg) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) X[j][DST] = make_float2(__fmul_rn(sg, X[j][SRC].x), __fmul_rn(sg, X[j][SRC].y));
+}
+
+// The in-thread part of the reference's edge fill on the previous sweep's values:
+// left/right edge columns from their inner column, top/bottom edge rows from their
+// inner row, where both lie in this thread's block. Corner and outside cells this also
+// writes are never read by interior cells.
+__device__ __forceinline__ void fill_in_thread(float2 (&X)[4][4], const EdgeGeom& g) {
+    switch (g.q1) {  // grid column 0 = block column q1 - 1
+        case 1: fill_col<0, 1>(X, g.s_lr); break;
+        case 2: fill_col<1, 2>(X, g.s_lr); break;
+        case 3: fill_col<2, 3>(X, g.s_lr); break;
+        default: break;
+    }
+    switch (g.q2) {  // grid column cols - 1 = block column q2 + 1
+        case 0: fill_col<1, 0>(X, g.s_lr); break;
+        case 1: fill_col<2, 1>(X, g.s_lr); break;
+        case 2: fill_col<3, 2>(X, g.s_lr); break;
+        default: break;
+    }
+    switch (g.i1) {  // grid row 0 = block row i1 - 1
+        case 1: fill_row<0, 1>(X, g.s_tb); break;
+        case 2: fill_row<1, 2>(X, g.s_tb); break;
+        case 3: fill_row<2, 3>(X, g.s_tb); break;
+        case 4: fill_row<3, 4>(X, g.s_tb); break;
+        case 5: fill_row<4, 5>(X, g.s_tb); break;
+        case 6: fill_row<5, 6>(X, g.s_tb); break;
+        case 7: fill_row<6, 7>(X, g.s_tb); break;
+        default: break;
+    }
+    switch (g.i2) {  // grid row rows - 1 = block row i2 + 1
+        case 0: fill_row<1, 0>(X, g.s_tb); break;
+        case 1: fill_row<2, 1>(X, g.s_tb); break;
+        case 2: fill_row<3, 2>(X, g.s_tb); break;
+        case 3: fill_row<4, 3>(X, g.s_tb); break;
+        case 4: fill_row<5, 4>(X, g.s_tb); break;
+        case 5: fill_row<6, 5>(X, g.s_tb); break;
+        case 6: fill_row<7, 6>(X, g.s_tb); break;
+        default: break;
+    }
+}
+
+// One sweep X -> Y. K: this thread's constant terms (kidx layout, warp block base +
+// 4 * lane); E: the exchange buffer of this sweep; my_top/my_bot/nb_up/nb_dn: offsets of
+// this warp's published rows and of the neighbours' rows in it.
+template <bool DIFF, bool EDGE>
+__device__ __forceinline__ void sweep(float2 (&X)[4][4], float2 (&Y)[4][4], const float* __restrict__ K,
+                                      float* __restrict__ E, int my_top, int my_bot, int nb_up, int nb_dn, bool fold,
+                                      const EdgeGeom& g, const Coef2& c) {
     constexpr int RW = kRegionW;
     constexpr unsigned FULL = 0xffffffffu;
+    if (EDGE && fold) fill_in_thread(X, g);
+    *reinterpret_cast<float4*>(E + my_top) = make_float4(X[0][0].x, X[0][1].x, X[0][2].x, X[0][3].x);
+    *reinterpret_cast<float4*>(E + my_bot) = make_float4(X[3][0].y, X[3][1].y, X[3][2].y, X[3][3].y);
+    __syncthreads();
+    const float4 u4 = *reinterpret_cast<const float4*>(E + nb_up);
+    const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn);
+    float up[4] = {u4.x, u4.y, u4.z, u4.w}, dn[4] = {d4.x, d4.y, d4.z, d4.w};
+    if (EDGE && fold) {
+        if (g.i1 == 0) {  // grid row 0 is the row above this block
+#pragma unroll
+            for (int q = 0; q < 4; ++q) up[q] = __fmul_rn(g.s_tb, X[0][q].x);
+        }
+        if (g.i2 == 7) {  // grid row rows - 1 is the row below this block
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dn[q] = __fmul_rn(g.s_tb, X[3][q].y);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float2 L0 = make_float2(__shfl_up_sync(FULL, X[j][3].x, 1), __shfl_up_sync(FULL, X[j][3].y, 1));
+        float2 R3 = make_float2(__shfl_down_sync(FULL, X[j][0].x, 1), __shfl_down_sync(FULL, X[j][0].y, 1));
+        if (EDGE && fold) {
+            if (g.q1 == 0) L0 = make_float2(__fmul_rn(g.s_lr, X[j][0].x), __fmul_rn(g.s_lr, X[j][0].y));
+            if (g.q2 == 3) R3 = make_float2(__fmul_rn(g.s_lr, X[j][3].x), __fmul_rn(g.s_lr, X[j][3].y));
+        }
+        const float4 ka = *reinterpret_cast<const float4*>(K + j * (2 * RW));
+        const float4 kb = *reinterpret_cast<const float4*>(K + j * (2 * RW) + RW);
+        const float2 kk[4] = {make_float2(ka.x, ka.y), make_float2(ka.z, ka.w), make_float2(kb.x, kb.y),
+                              make_float2(kb.z, kb.w)};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 L = q > 0 ? X[j][q - 1] : L0;
+            const float2 R = q < 3 ? X[j][q + 1] : R3;
+            const float2 U = j > 0 ? X[j - 1][q] : make_float2(up[q], X[3][q].x);
+            const float2 D = j < 3 ? X[j + 1][q] : make_float2(X[0][q].y, dn[q]);
+            Y[j][q] = update2<DIFF>(kk[q], L, R, U, D, c);
+        }
+    }
+}
+
+template <bool DIFF, bool EDGE, int NW>
+__device__ __forceinline__ void run_sweeps(float2 (&X)[4][4], int koff, int eoff, int nsweeps, int w, int lane,
+                                           const EdgeGeom& g, const Coef2& c) {
+    constexpr int RW = kRegionW;
     extern __shared__ float4 smem4[];
-    float* const E = reinterpret_cast<float*>(smem4) + eoff;
-    const float* const K = reinterpret_cast<const float*>(smem4) + koff + (w * SRB) * RW + 4 * lane;
+    float* const S = reinterpret_cast<float*>(smem4);
+    const float* const K = S + koff + w * (8 * RW) + 4 * lane;
+    float* const E0 = S + eoff;
+    float* const E1 = E0 + 2 * NW * RW;  // the second exchange buffer
     const int my_top = (2 * w) * RW + 4 * lane;
     const int my_bot = my_top + RW;
     // bottom row of warp w - 1 and top row of warp w + 1; the first and last warps read
     // their own rows instead (the region border, whose values nothing stored uses)
     const int nb_up = w > 0 ? my_top - RW : my_top;
     const int nb_dn = w < NW - 1 ? my_top + 2 * RW : my_bot;
-    constexpr int EB = 2 * NW * RW;     // floats per exchange buffer
+    float2 Y[4][4];
+    int s = 0;
 #pragma unroll 1
-    for (int s = 0; s < nsweeps; ++s) {
-        const int eo = (s & 1) * EB;
-        *reinterpret_cast<float4*>(E + my_top + eo) = make_float4(x[0][0], x[0][1], x[0][2], x[0][3]);
-        *reinterpret_cast<float4*>(E + my_bot + eo) = make_float4(x[SRB - 1][0], x[SRB - 1][1], x[SRB - 1][2],
-                                                              x[SRB - 1][3]);
-        __syncthreads();
-        float up[4], dn[4];
-        {
-            const float4 u4 = *reinterpret_cast<const float4*>(E + nb_up + eo);
-            const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn + eo);
-            up[0] = u4.x, up[1] = u4.y, up[2] = u4.z, up[3] = u4.w;
-            dn[0] = d4.x, dn[1] = d4.y, dn[2] = d4.z, dn[3] = d4.w;
-        }
-        const bool fold = EDGE && s > 0;
-        float prev[4] = {up[0], up[1], up[2], up[3]};  // previous sweep's row i - 1
+    for (; s + 1 < nsweeps; s += 2) {
+        sweep<DIFF, EDGE>(X, Y, K, E0, my_top, my_bot, nb_up, nb_dn, s > 0, g, c);
+        sweep<DIFF, EDGE>(Y, X, K, E1, my_top, my_bot, nb_up, nb_dn, true, g, c);
+    }
+    if (s < nsweeps) {
+        sweep<DIFF, EDGE>(X, Y, K, E0, my_top, my_bot, nb_up, nb_dn, s > 0, g, c);
 #pragma unroll
-        for (int i = 0; i < SRB; ++i) {
-            float cur[4], below[4];
+        for (int j = 0; j < 4; ++j)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                cur[q] = x[i][q];
-                below[q] = i + 1 < SRB ? x[i + 1][q] : dn[q];
-            }
-            const float lsh = __shfl_up_sync(FULL, cur[3], 1);
-            const float rsh = __shfl_down_sync(FULL, cur[0], 1);
-            const float4 k4 = *reinterpret_cast<const float4*>(K + i * RW);
-            const float kr[4] = {k4.x, k4.y, k4.z, k4.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                float L = q > 0 ? cur[q - 1] : lsh;
-                float R = q < 3 ? cur[q + 1] : rsh;
-                float U = prev[q], D = below[q];
-                if (EDGE && fold) {
-                    if (i == i1) U = __fmul_rn(s_tb, cur[q]);
-                    if (i == i2) D = __fmul_rn(s_tb, cur[q]);
-                    if (q == q1) L = __fmul_rn(s_lr, cur[q]);
-                    if (q == q2) R = __fmul_rn(s_lr, cur[q]);
-                }
-                float nv = DIFF ? diffuse_update(kr[q], L, R, U, D, a, dh, dl, rf) : pressure_update(kr[q], L, R, U, D);
-                if (EDGE) nv = (((row_int >> i) & (col_int >> q)) & 1u) ? nv : cur[q];
-                x[i][q] = nv;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) prev[q] = cur[q];
-        }
+            for (int q = 0; q < 4; ++q) X[j][q] = Y[j][q];
     }
 }
 
@@ -212,42 +306,48 @@ struct SweepParams {
     float s_lr, s_tb, a, dh, dl, rf;
 };
 
-// The sweeps of one tile in the block layout of run_sweeps: the field (X) and its
-// constant term (K) go from shared memory into registers, the sweeps run, and the final
-// field goes back to X. Kept out of line so that the tile body's other live values are
-// saved once around the call instead of competing with the register blocks.
-template <bool DIFF, int NW, int SRB>
+// The sweeps of one tile in the block layout of run_sweeps: the field goes from shared
+// memory (row-major at xoff) into registers, the sweeps run (constant terms read at koff
+// in the kidx layout, the exchange area overlaying the field's buffer), and the final
+// field goes back to xoff. Kept out of line so that the tile body's other live values
+// are saved once around the call instead of competing with the register blocks.
+template <bool DIFF, int NW>
 __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P) {
     constexpr int RW = kRegionW;
     extern __shared__ float4 smem4[];
     float* const X = reinterpret_cast<float*>(smem4) + xoff;
     const int tid = threadIdx.y * RW + threadIdx.x;
     const int w = tid >> 5, lane = tid & 31;
-    const int rb = w * SRB, cb = 4 * lane;
-    float xb[SRB][4];
+    const int rb = w * 8, cb = 4 * lane;
+    float2 xb[4][4];
 #pragma unroll
-    for (int i = 0; i < SRB; ++i) {
-        const float4 t = *reinterpret_cast<const float4*>(X + (rb + i) * RW + cb);
-        xb[i][0] = t.x, xb[i][1] = t.y, xb[i][2] = t.z, xb[i][3] = t.w;
+    for (int j = 0; j < 4; ++j) {
+        const float4 t = *reinterpret_cast<const float4*>(X + (rb + j) * RW + cb);
+        const float4 b = *reinterpret_cast<const float4*>(X + (rb + j + 4) * RW + cb);
+        xb[j][0] = make_float2(t.x, b.x);
+        xb[j][1] = make_float2(t.y, b.y);
+        xb[j][2] = make_float2(t.z, b.z);
+        xb[j][3] = make_float2(t.w, b.w);
     }
-    __syncthreads();  // the exchange area of the sweeps overlays X
+    __syncthreads();  // the exchange area of the sweeps overlays the field's buffer
+    const Coef2 c = {make_float2(P.a, P.a), make_float2(-P.dh, -P.dh), make_float2(-P.dl, -P.dl),
+                     make_float2(P.rf, P.rf)};
     if (P.edge) {
         const int gyb = P.gy0 + rb, gxb = P.gx0 + cb;
-        unsigned row_int = 0, col_int4 = 0;
-#pragma unroll
-        for (int i = 0; i < SRB; ++i) row_int |= (unsigned)(gyb + i >= 1 && gyb + i <= P.rows - 2) << i;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) col_int4 |= (unsigned)(gxb + q >= 1 && gxb + q <= P.cols - 2) << q;
-        run_sweeps<DIFF, true, NW, SRB>(xb, koff, xoff, P.nsweeps, w, lane, row_int, col_int4, 1 - gyb, P.rows - 2 - gyb,
-                                        1 - gxb, P.cols - 2 - gxb, P.s_lr, P.s_tb, P.a, P.dh, P.dl, P.rf);
+        const EdgeGeom g = {1 - gyb, P.rows - 2 - gyb, 1 - gxb, P.cols - 2 - gxb, P.s_lr, P.s_tb};
+        run_sweeps<DIFF, true, NW>(xb, koff, xoff, P.nsweeps, w, lane, g, c);
     } else {
-        run_sweeps<DIFF, false, NW, SRB>(xb, koff, xoff, P.nsweeps, w, lane, 0u, 0u, -1, -1, -1, -1, P.s_lr, P.s_tb, P.a,
-                                         P.dh, P.dl, P.rf);
+        const EdgeGeom g = {-1, -1, -1, -1, P.s_lr, P.s_tb};
+        run_sweeps<DIFF, false, NW>(xb, koff, xoff, P.nsweeps, w, lane, g, c);
     }
     __syncthreads();  // every warp has read its last exchange rows
 #pragma unroll
-    for (int i = 0; i < SRB; ++i)
-        *reinterpret_cast<float4*>(X + (rb + i) * RW + cb) = make_float4(xb[i][0], xb[i][1], xb[i][2], xb[i][3]);
+    for (int j = 0; j < 4; ++j) {
+        *reinterpret_cast<float4*>(X + (rb + j) * RW + cb) =
+            make_float4(xb[j][0].x, xb[j][1].x, xb[j][2].x, xb[j][3].x);
+        *reinterpret_cast<float4*>(X + (rb + j + 4) * RW + cb) =
+            make_float4(xb[j][0].y, xb[j][1].y, xb[j][2].y, xb[j][3].y);
+    }
     __syncthreads();
 }
 
@@ -266,7 +366,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // arithmetic, the epilogues) and the block layout of run_sweeps.
     constexpr int RW = kRegionW, NW = 4 * TY, RH = NW * SRB, SR = RH / TY;
     static_assert(SR <= 32, "column-layout row masks are 32-bit");
-    static_assert(SRB >= 4, "the sweep exchange area must fit in one region buffer");
+    static_assert(SRB == 8, "run_sweeps holds 8 rows per warp");
     extern __shared__ float4 smem4[];
     float* const S = reinterpret_cast<float*>(smem4);
     constexpr int co = 0, no = RH * RW;  // S + co: the field; S + no: its constant term
@@ -286,7 +386,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txl = tx > 0 ? tx - 1 : 0;
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
 
-#define KREF(i) (S[no + (r0 + (i)) * RW + tx])
+#define KREF(i) (S[no + kidx(r0 + (i), tx)])
 #define XREF(i) (S[co + (r0 + (i)) * RW + tx])
 
     // Row masks of this thread's column segment (bit i = row r0 + i of the region),
@@ -335,7 +435,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         for (int i = 0; i < SR; ++i) {
             S[co + (r0 + i) * RW + tx] =
                 (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
-            S[no + (r0 + i) * RW + tx] = kc[i];
+            KREF(i) = kc[i];
         }
     } else if (kind == PASS_DIFFUSE_FIRST) {
         // add_sources_kernel (fluid_solver_gpu.cu:64) fused into the load
@@ -346,14 +446,14 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
             if ((m_int >> i) & 1u) x = __fmaf_rn(dt, __ldcg(F.x2 + o), x);  // fused, as compiled
             S[co + (r0 + i) * RW + tx] = x;
-            S[no + (r0 + i) * RW + tx] = x;
+            KREF(i) = x;
         }
     } else {
 #pragma unroll
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
             S[co + (r0 + i) * RW + tx] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            S[no + (r0 + i) * RW + tx] = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
+            KREF(i) = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
         }
     }
     __syncthreads();
@@ -362,8 +462,22 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
     if (F.sweeps > 0) {
         const SweepParams P = {F.sweeps, edge_cta ? 1 : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
-        sweep_phase<DIFF, NW, SRB>(co, no, P);
-        if (edge_cta) fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
+        sweep_phase<DIFF, NW>(co, no, P);
+        if (edge_cta) {
+            fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
+            // restore_corners: the reference never writes the four corners; the sweeps
+            // computed values there that nothing read, so put the pass's input back
+            if (gc == 0 || gc == cols - 1) {
+                const float* src = kind == PASS_PRESSURE_FIRST ? F.cst : xin;
+#pragma unroll
+                for (int i = 0; i < SR; ++i) {
+                    const int gr = g0 + i;
+                    if (gr == 0 || gr == rows - 1)
+                        XREF(i) = src ? __ldcg(src + o0 + (size_t)i * pitch) : 0.f;
+                }
+            }
+            __syncthreads();
+        }
     }
     // final values of this thread's column: XREF(i) (S + co is complete after the last barrier)
 
@@ -396,7 +510,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         // Rows go in batches of EB: first the cell each row reads u and v from (its own,
         // or its inner neighbour's on an edge) for the whole batch, so the global loads
         // are in flight together, then the arithmetic, in the reference's order.
-        constexpr int EB = 8;
+        constexpr int EB = SR;
     #pragma unroll
         for (int i0 = 0; i0 < SR; i0 += EB) {
             float uin[EB], vin[EB];

@@ -271,11 +271,16 @@ FS_API int fs_batch_sync(fs_batch* b);
 FS_API int fs_batch_get_stats(const fs_batch* b, fs_stats* out);
 FS_API int fs_batch_stream(fs_batch* b, void** stream);
 
-/* Per-kernel timing of one step. The step runs eagerly (not from the graph) with a
- * CUDA event recorded on the handle's stream around every launch; for each kernel kind
- * the result holds the launch count, the summed event time and the algorithmic bytes
- * (each input field read once and each output written once per sweep, the cost model
- * of the reference's one-kernel-per-sweep design). The state advances by one step. */
+/* Per-kernel timing of one step. The step runs eagerly (not from the graph) in the
+ * graph's shape — the same launches on the same streams, the density branch beside the
+ * main stream — with a CUDA event recorded around every launch on the stream it runs
+ * on. For each kernel kind: the launch count and summed event time, the part of both
+ * that ran on the density branch (concurrently with the main stream, so the main
+ * stream's total ms - branch_ms never exceeds the step), the algorithmic bytes of the
+ * per-sweep model (each input field read once and each output written once per sweep,
+ * the cost of the reference's one-kernel-per-sweep design) and the pass bytes (each
+ * array a launch itself reads or writes, once: what a temporally blocked pass must move
+ * through HBM). The state advances by one step. */
 #define FS_KIND_STENCIL 0   /* diffusion / pressure passes (temporally blocked) */
 #define FS_KIND_SPLAT 1     /* forward density advection */
 #define FS_KIND_FINISH 2    /* density fill + smoothing */
@@ -286,6 +291,9 @@ typedef struct fs_kernel_times {
     int launches[FS_NUM_KINDS];
     double ms[FS_NUM_KINDS];
     double algorithmic_bytes[FS_NUM_KINDS];
+    double pass_bytes[FS_NUM_KINDS];
+    int branch_launches[FS_NUM_KINDS];
+    double branch_ms[FS_NUM_KINDS];
 } fs_kernel_times;
 FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float dt, fs_kernel_times* out);
 

@@ -2,7 +2,6 @@
 before any CUDA call, and the product fails loudly (never silently) without a device.
 With a GPU (marked gpu), the C++ adapter is built and driven like the reference app."""
 import ctypes as C
-import os
 import pathlib
 import re
 import subprocess
@@ -85,7 +84,9 @@ def _build_adapter(tmp_path, include_dirs, extra=()):
 
 
 def test_adapter_builds_against_reference_headers(fluid, tmp_path):
-    ref = pathlib.Path(os.environ.get("FLUID2D_REF_SRC", "/root/reference/src"))
+    from oracle import build_oracle
+
+    ref = build_oracle.REF_SRC  # the reference checkout the oracle recipe builds from
     if not (ref / "fluid_solver.hpp").exists():
         pytest.skip("reference sources not present on this machine")
     exe = _build_adapter(tmp_path, [ref], extra=("-include", "cstddef"))

@@ -32,7 +32,9 @@ def test_forward_and_gradients_match_cpu_reference(fluid):
     x0 = torch.from_numpy(x0).to(torch.bfloat16).float().numpy()
     target = rng.standard_normal((B, G, G)).astype(np.float32)
     # CPU reference, FP64 with BF16 weights / activations
-    y_ref, ps = Lm.cpu_forward(params, x0)
+    from net_reference import cpu_forward
+
+    y_ref, ps = cpu_forward(params, x0)
     loss = ((y_ref[..., 0] - torch.from_numpy(target).double()) ** 2).mean()
     loss.backward()
     g_ref = np.concatenate([np.concatenate([w.grad.numpy().ravel(), b.grad.numpy().ravel()]) for w, b in ps])
