@@ -43,7 +43,8 @@ class fs_config(C.Structure):
                 ("tile_rows", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("warm_start", C.c_int),
                 ("pressure_tolerance", C.c_float), ("pressure_max_iterations", C.c_int),
                 ("check_finite", C.c_int), ("capture", C.c_int), ("method", C.c_int),
-                ("learned_cycles", C.c_int), ("learned_cycle_iterations", C.c_int), ("learned_grid", C.c_int)]
+                ("learned_cycles", C.c_int), ("learned_cycle_iterations", C.c_int), ("learned_grid", C.c_int),
+                ("learned_defect", C.c_int)]
 
 
 class fs_stats(C.Structure):

@@ -180,6 +180,12 @@ cudaError_t launch_damp(const float* div, const float* p, float* out, int rows, 
                         const int* skip_if, cudaStream_t st);
 cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float* p_try, int rows, int cols,
                                int pitch, double* out, const int* skip_if, cudaStream_t st);
+// Mixed-precision defect correction (net.cu): r = residual of p_hi + p_lo in FP64
+// (stored FP32; sums[0] += ||r||^2, sums[1] += ||div||^2, zeroed before), and
+// (p_hi, p_lo) += e with the sum split back into two floats.
+cudaError_t launch_residual_df(const float* div, const float* p_hi, const float* p_lo, float* r, int rows, int cols,
+                               int pitch, double* sums, cudaStream_t st);
+cudaError_t launch_accumulate_df(float* p_hi, float* p_lo, const float* e, long n_floats, cudaStream_t st);
 cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, long n_floats, const double* gain,
                                const int* converged, unsigned long long* counters, cudaStream_t st);
 

@@ -10,6 +10,7 @@
 // No counterpart in the reference (it has no learned component).
 
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "../../include/fluid2d_gb300.h"
@@ -436,6 +437,65 @@ __global__ void accept_best_kernel(float* __restrict__ p_cur, const float* __res
         dst[e] = src[e];
 }
 
+// ------------------------------------------------------- defect correction
+// Mixed-precision defect correction of a residual-driven projection. The pressure is
+// kept as an unevaluated sum p_hi + p_lo of two FP32 fields; each cycle forms the
+// residual of that sum in FP64, solves the correction e in FP32 (network + Jacobi, from
+// e = 0) and adds it back exactly. The FP32 iteration alone stalls once the residual
+// nears its rounding floor (about 4 eps |p| per cell, far above 1e-4 ||div|| when the
+// divergence is smooth); the correction's own floor is relative to |e|, so each cycle
+// gains a further factor.
+//
+// r = div + sum(nbrs (p_hi + p_lo)) - 4 (p_hi + p_lo) on the interior in FP64, stored in
+// FP32 (edges 0); sums[0] += ||r||^2, sums[1] += ||div||^2 (FP64, zeroed before).
+__global__ void residual_df_kernel(const float* __restrict__ div, const float* __restrict__ ph,
+                                   const float* __restrict__ pl, float* __restrict__ r, int rows, int cols, int pitch,
+                                   double* __restrict__ sums) {
+    __shared__ double red[2][256];
+    double rr = 0.0, dd = 0.0;
+    const long n = (long)rows * cols;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / cols), j = (int)(e % cols);
+        const size_t o = (size_t)i * pitch + j;
+        if (i < 1 || i > rows - 2 || j < 1 || j > cols - 2) {
+            r[o] = 0.f;
+            continue;
+        }
+        auto P = [&](size_t q) { return (double)ph[q] + (double)pl[q]; };
+        const double dv = (double)div[o];
+        const double res = dv + ((P(o - 1) + P(o + 1)) + (P(o - pitch) + P(o + pitch))) - 4.0 * P(o);
+        r[o] = (float)res;
+        rr += res * res;
+        dd += dv * dv;
+    }
+    red[0][threadIdx.x] = rr;
+    red[1][threadIdx.x] = dd;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + s];
+            red[1][threadIdx.x] += red[1][threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(sums, red[0][0]);
+        atomicAdd(sums + 1, red[1][0]);
+    }
+}
+
+// (p_hi, p_lo) += e: t = p_hi + p_lo + e in FP64, p_hi = RN(t), p_lo = RN(t - p_hi), on
+// every cell (edges included, so both parts keep their Neumann fill).
+__global__ void accumulate_df_kernel(float* __restrict__ ph, float* __restrict__ pl, const float* __restrict__ e,
+                                     long n) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+        const double t = ((double)ph[k] + (double)pl[k]) + (double)e[k];
+        const float hi = (float)t;
+        ph[k] = hi;
+        pl[k] = (float)(t - (double)hi);
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, int cols, int pitch, int G, float* bs,
@@ -494,6 +554,20 @@ cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float
 cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, long n_floats, const double* gain,
                                const int* converged, unsigned long long* counters, cudaStream_t st) {
     accept_best_kernel<<<152 * 4, 256, 0, st>>>(p_cur, pa, pb, n_floats / 4, gain, converged, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_residual_df(const float* div, const float* p_hi, const float* p_lo, float* r, int rows, int cols,
+                               int pitch, double* sums, cudaStream_t st) {
+    const long n = (long)rows * cols;
+    const int blocks = (int)std::min<long>((n + 255) / 256, 4096);
+    residual_df_kernel<<<blocks, 256, 0, st>>>(div, p_hi, p_lo, r, rows, cols, pitch, sums);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_df(float* p_hi, float* p_lo, const float* e, long n_floats, cudaStream_t st) {
+    const int blocks = (int)std::min<long>((n_floats + 255) / 256, 8192);
+    accumulate_df_kernel<<<blocks, 256, 0, st>>>(p_hi, p_lo, e, n_floats);
     return cudaGetLastError();
 }
 

@@ -138,6 +138,9 @@ struct fs_solver {
         void* mem = nullptr;
     } net;
     float* pguess = nullptr;  // fine starting pressure built from the network
+    float* plo = nullptr;     // learned residual solves: low part of the pressure (p_hi + p_lo)
+    float* rhs = nullptr;     // learned residual solves: FP64-formed residual, the correction's right side
+    float* ecur = nullptr;    // learned residual solves: the correction being solved for
     SolveCtrl* host_ctrl = nullptr;  // pinned mirror of a control block (learned cycles)
     fs_source_event* d_events = nullptr;  // device copy of a source script
     int d_events_cap = 0;
@@ -284,7 +287,8 @@ int prof_begin(fs_solver* s, cudaStream_t st) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     s->prof_events.push_back(e);
-    CK(cudaEventRecord(e, st));
+    // an event-record node when the profiled step is being captured (fs_profile_step)
+    CK(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
     return FS_OK;
 }
 
@@ -295,7 +299,7 @@ int prof_end(fs_solver* s, cudaStream_t st, int kind, double bytes, double pass_
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
     s->prof_events.push_back(e);
-    CK(cudaEventRecord(e, st));
+    CK(cudaEventRecordWithFlags(e, st, cudaEventRecordExternal));
     s->prof_marks.push_back({kind, bytes, pass_bytes, st != s->stream});
     return FS_OK;
 }
@@ -413,24 +417,26 @@ constexpr int kCoarseSweepsFine = 200;  // on the finer coarse level
 // the classical candidate (the coarse smoothing from zero, no network). The acceptance rule keeps
 // the candidate that brings p_cur closest to the solution in the A-norm (the norm the
 // Jacobi iteration contracts), or p_cur when neither gets closer, and counts whether the
-// network's candidate won. Does nothing to p_cur once *converged (nullable) is set.
-int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged, Counter& cnt) {
+// network's candidate won. Does nothing to p_cur once *converged (nullable) is set. rhs is
+// the right side of the problem p_cur approximates: the divergence, or in a defect
+// correction cycle the residual the correction solves for.
+int enqueue_network_correction(fs_solver* s, const float* rhs, float* p_cur, const int* converged, Counter& cnt) {
     const int G = s->net.G;
     // one damped Jacobi step first: removes the checkerboard error plain Jacobi never damps
-    CK(launch_damp(s->div, p_cur, s->p[0], s->rows, s->cols, s->pitch, converged, s->stream));
-    CK(launch_damp(s->div, s->p[0], p_cur, s->rows, s->cols, s->pitch, converged, s->stream));
+    CK(launch_damp(rhs, p_cur, s->p[0], s->rows, s->cols, s->pitch, converged, s->stream));
+    CK(launch_damp(rhs, s->p[0], p_cur, s->rows, s->cols, s->pitch, converged, s->stream));
     cnt.launches += 2;
     const float kappa = net_kappa(G);
     const int G2 = s->net.G2;
     if (G2) {
         // block sums on the finer level, summed up for the network's level
-        CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G2, s->net.bs2, nullptr, s->net.scale2,
+        CK(launch_coarse_residual(rhs, p_cur, s->rows, s->cols, s->pitch, G2, s->net.bs2, nullptr, s->net.scale2,
                                   nullptr, converged, s->stream));
         CK(launch_coarse_sum2x2(s->net.bs2, s->net.bs, G, converged, s->stream));
         CK(launch_coarse_input(s->net.bs, G, s->net.scale, net_act(s, 0), s->net.res, converged, s->stream));
         cnt.launches += 4;
     } else {
-        CK(launch_coarse_residual(s->div, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
+        CK(launch_coarse_residual(rhs, p_cur, s->rows, s->cols, s->pitch, G, s->net.bs, s->net.res, s->net.scale,
                                   net_act(s, 0), converged, s->stream));
         cnt.launches += 2;
     }
@@ -480,8 +486,8 @@ int enqueue_network_correction(fs_solver* s, float* p_cur, const int* converged,
                           s->stream));
     }
     CK(cudaMemsetAsync(s->net.res + 1, 0, 2 * sizeof(double), s->stream));
-    CK(launch_energy_gain(s->div, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
-    CK(launch_energy_gain(s->div, p_cur, pb, s->rows, s->cols, s->pitch, s->net.res + 2, converged, s->stream));
+    CK(launch_energy_gain(rhs, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
+    CK(launch_energy_gain(rhs, p_cur, pb, s->rows, s->cols, s->pitch, s->net.res + 2, converged, s->stream));
     CK(launch_accept_best(p_cur, s->pguess, pb, (long)s->field_floats, s->net.res + 1, converged, s->net.counters,
                           s->stream));
     cnt.launches += 9;
@@ -494,7 +500,7 @@ int enqueue_learned_guess(fs_solver* s, const float* u_in, const float* v_in, in
     int rc = enqueue_div_pass(s, u_in, v_in, cnt);
     if (rc != FS_OK) return rc;
     if (!s->warm_valid) CK(cudaMemsetAsync(s->pwarm[slot], 0, s->field_floats * sizeof(float), s->stream));
-    return enqueue_network_correction(s, s->pwarm[slot], nullptr, cnt);
+    return enqueue_network_correction(s, s->div, s->pwarm[slot], nullptr, cnt);
 }
 
 // Starting pressure of projection `slot`: the network's guess, the previous pressure,
@@ -599,7 +605,7 @@ int enqueue_project_learned_cycles(fs_solver* s, const float* u_in, const float*
     P.p_cur = pcur;
     const int blocks = std::min(s->solve_blocks, P.mid.tiles_x * P.mid.tiles_y);
     for (int c = 0; c < cycles; ++c) {
-        if ((rc = enqueue_network_correction(s, pcur, &P.ctrl->converged, cnt)) != FS_OK) return rc;
+        if ((rc = enqueue_network_correction(s, s->div, pcur, &P.ctrl->converged, cnt)) != FS_OK) return rc;
         const int budget = c + 1 < cycles ? per : std::max(per, cap - (cycles - 1) * per);
         P.max_passes = std::max(1, (budget + K - 1) / K);
         PROF_BEGIN(s);
@@ -617,10 +623,106 @@ int enqueue_project_learned_cycles(fs_solver* s, const float* u_in, const float*
     return capture_div(s, slot);
 }
 
+// Residual-driven projection with learned corrections as mixed-precision defect
+// correction (outside a stream capture). The pressure is p_hi + p_lo (pwarm[slot] and
+// plo): each cycle forms the residual r of that sum in FP64 (launch_residual_df), stops
+// when ||r|| / ||div|| <= tol, and otherwise solves A e = r for a correction e in FP32 —
+// from e = 0, one network correction (the same cycle as below, on r) and a segment of
+// Jacobi passes until ||r - A e|| <= tol ||div|| or the segment's budget — and adds e to
+// the pressure exactly (launch_accumulate_df). The FP32 iterate alone stalls near its
+// rounding floor (about 4 eps |p| per cell); the correction's floor is relative to |e|,
+// so the residual keeps falling cycle after cycle. The velocity is then corrected with
+// p_hi, the pressure rounded to FP32 as the reference stores it.
+int enqueue_project_learned_defect(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
+                                   int slot, Counter& cnt) {
+    const int K = s->sweeps;
+    const int per = s->cfg.learned_cycle_iterations > 0 ? s->cfg.learned_cycle_iterations : 128;
+    const int cap = s->cfg.pressure_max_iterations;
+    const int cycles = s->cfg.learned_cycles > 0 ? s->cfg.learned_cycles : std::max(1, (cap + per - 1) / per);
+    const double tol = s->cfg.pressure_tolerance;
+    int rc = enqueue_div_pass(s, u_in, v_in, cnt);
+    if (rc != FS_OK) return rc;
+    float* phi = s->pwarm[slot];
+    const size_t fbytes = s->field_floats * sizeof(float);
+    if (!s->warm_valid) CK(cudaMemsetAsync(phi, 0, fbytes, s->stream));
+    CK(cudaMemsetAsync(s->plo, 0, fbytes, s->stream));
+    if (s->cfg.capture) CK(cudaMemcpyAsync(s->cap_start[slot], phi, fbytes, cudaMemcpyDeviceToDevice, s->stream));
+    double* dsums = reinterpret_cast<double*>(s->flags + 4);  // two doubles in the flag block
+    double* hsums = reinterpret_cast<double*>(s->host_ctrl + 1);
+    PressureSolve P{};
+    set_geometry(P.mid, s, K + 1);
+    P.mid.s_lr = P.mid.s_tb = 1.f;
+    P.mid.sweeps = K;
+    P.mid.h = grid_h(s->rows, s->cols);
+    P.mid.kind = PASS_PRESSURE;
+    P.mid.cst = s->rhs;
+    P.first = P.mid;
+    P.first.x = s->ecur;
+    P.p[0] = s->p[0];
+    P.p[1] = s->p[1];
+    P.partials = s->partials[slot];
+    P.ctrl = s->ctrl + slot;
+    P.poll_limit = reinterpret_cast<const unsigned*>(s->flags + 1);
+    P.segment = 1;
+    P.p_cur = s->ecur;
+    const int blocks = std::min(s->solve_blocks, P.mid.tiles_x * P.mid.tiles_y);
+    int passes = 0, used = 0;
+    double ratio = 1.0;
+    bool converged = false, timed_out = false;
+    for (int c = 0; c <= cycles; ++c) {
+        CK(cudaMemsetAsync(dsums, 0, 2 * sizeof(double), s->stream));
+        CK(launch_residual_df(s->div, phi, s->plo, s->rhs, s->rows, s->cols, s->pitch, dsums, s->stream));
+        CK(cudaMemcpyAsync(hsums, dsums, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        cnt.launches++;
+        ratio = hsums[1] > 0.0 ? std::sqrt(hsums[0] / hsums[1]) : std::sqrt(hsums[0]);
+        converged = ratio <= tol;
+        if (converged || c == cycles || used >= cap) break;
+        // the correction: from zero, to the residual that would meet the target
+        CK(cudaMemsetAsync(s->ecur, 0, fbytes, s->stream));
+        CK(cudaMemsetAsync(P.ctrl, 0, sizeof(SolveCtrl), s->stream));
+        if ((rc = enqueue_network_correction(s, s->rhs, s->ecur, nullptr, cnt)) != FS_OK) return rc;
+        const int budget = std::min(per, cap - used);
+        P.max_passes = std::max(1, (budget + K - 1) / K);
+        P.tol = (float)std::min(0.5, hsums[0] > 0.0 ? tol * std::sqrt(hsums[1] / hsums[0]) : 1.0);
+        PROF_BEGIN(s);
+        CK(launch_pressure_solve(P, s->tile_rows, blocks, s->stream));
+        PROF_END(s, FS_KIND_STENCIL, 0.0);  // bytes depend on the iteration count reached
+        cnt.launches++;
+        cnt.passes++;
+        CK(cudaMemcpyAsync(s->host_ctrl, P.ctrl, sizeof(SolveCtrl), cudaMemcpyDeviceToHost, s->stream));
+        CK(launch_accumulate_df(phi, s->plo, s->ecur, (long)s->field_floats, s->stream));
+        cnt.launches++;
+        CK(cudaStreamSynchronize(s->stream));
+        passes += s->host_ctrl->passes;
+        used += s->host_ctrl->passes * K;
+        if (s->host_ctrl->error) {
+            timed_out = true;
+            break;
+        }
+    }
+    // the outcome, where check_flags and fs_get_stats read it
+    SolveCtrl out{};
+    out.passes = passes;
+    out.converged = converged ? 1 : 0;
+    out.error = timed_out ? 1 : 0;
+    out.residual = ratio;
+    *s->host_ctrl = out;
+    CK(cudaMemcpyAsync(s->ctrl + slot, s->host_ctrl, sizeof(SolveCtrl), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if ((rc = enqueue_fin_pass(s, phi, u_in, v_in, u_out, v_out, cnt)) != FS_OK) return rc;
+    return capture_div(s, slot);
+}
+
 int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out,
                                 int slot, Counter& cnt) {
-    if (s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready)
+    if (s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready) {
+        cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(s->stream, &capture));
+        if (capture == cudaStreamCaptureStatusNone && s->host_ctrl != nullptr && s->cfg.learned_defect)
+            return enqueue_project_learned_defect(s, u_in, v_in, u_out, v_out, slot, cnt);
         return enqueue_project_learned_cycles(s, u_in, v_in, u_out, v_out, slot, cnt);
+    }
     const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
     const int K = s->sweeps;
@@ -1053,6 +1155,7 @@ int fs_config_init(fs_config* cfg, int rows, int cols) {
     cfg->pressure_tolerance = 0.f;
     cfg->pressure_max_iterations = 0;
     cfg->check_finite = 1;
+    cfg->learned_defect = 1;
     return FS_OK;
 }
 
@@ -1121,7 +1224,7 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
         return cuda_fail(e, "fs_create: stencil kernel set-up");
     }
     const bool learned = cfg->warm_start == FS_WARM_LEARNED;
-    const int nfields = 6 + 9 + 6 + 2 + (cfg->capture ? 4 : 0) + (learned ? 1 : 0);
+    const int nfields = 6 + 9 + 6 + 2 + (cfg->capture ? 4 : 0) + (learned ? 4 : 0);
     // tail: flags (256 B), two solve control blocks, two partial-sum arrays
     const size_t part_doubles = 4 * (size_t)std::max(1, s->solve_blocks);
     const size_t tail = 256 + 2 * 256 + 2 * part_doubles * sizeof(double);
@@ -1158,7 +1261,12 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
             s->cap_start[k] = take();
         }
     }
-    if (learned) s->pguess = take();
+    if (learned) {
+        s->pguess = take();
+        s->plo = take();
+        s->rhs = take();
+        s->ecur = take();
+    }
     char* tailp = reinterpret_cast<char*>(p);
     s->flags = reinterpret_cast<int*>(tailp);
     s->ctrl = reinterpret_cast<SolveCtrl*>(tailp + 256);
@@ -1216,7 +1324,8 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
                 rc = cuda_fail(e, "fs_create: network constants");
         }
     }
-    if (rc == FS_OK && learned && (e = cudaMallocHost(&s->host_ctrl, sizeof(SolveCtrl))) != cudaSuccess)
+    // a control block and, behind it, the two FP64 residual sums of a defect-correction cycle
+    if (rc == FS_OK && learned && (e = cudaMallocHost(&s->host_ctrl, 2 * sizeof(SolveCtrl))) != cudaSuccess)
         rc = cuda_fail(e, "fs_create: pinned control block");
     if (rc != FS_OK) {
         if (s->host_ctrl) cudaFreeHost(s->host_ctrl);
@@ -1565,9 +1674,31 @@ int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, float d
     s->prof_events.clear();
     s->prof_marks.clear();
     Counter cnt;
-    int rc = enqueue_step(s, diffusion_rate, viscosity, dt, cnt);
+    // The step is captured with an event-record node around every launch and replayed
+    // as one graph, so its launches follow one another as in the timed graph (no host
+    // launch latency between them); steps that read results on the host run eagerly.
+    const bool adaptive = s->cfg.warm_start == FS_WARM_LEARNED && s->net_ready && s->cfg.pressure_tolerance > 0.f;
+    int rc = FS_OK;
+    cudaError_t e = cudaSuccess;
+    if (!adaptive) {
+        cudaGraph_t gr = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = enqueue_step(s, diffusion_rate, viscosity, dt, cnt);
+            e = cudaStreamEndCapture(s->stream, &gr);
+        }
+        if (rc == FS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, gr, 0);
+        if (rc == FS_OK && e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
+        if (rc == FS_OK && e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (gr) cudaGraphDestroy(gr);
+        if (rc == FS_OK && e != cudaSuccess) rc = cuda_fail(e, "fs_profile_step: graph");
+    } else {
+        rc = enqueue_step(s, diffusion_rate, viscosity, dt, cnt);
+    }
     s->prof = nullptr;
-    cudaError_t e = cudaStreamSynchronize(s->stream);
+    e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->side);
     if (rc == FS_OK && e != cudaSuccess) rc = cuda_fail(e, "fs_profile_step: sync");
     if (rc == FS_OK) {

@@ -110,6 +110,22 @@ __device__ __forceinline__ int kidx(int r, int c) {
            (c & 1) * 2 + ((r >> 2) & 1);
 }
 
+// x / b correctly rounded, for b > 0 with y = RN(1/b): Markstein's correction step
+// (P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): q0 = RN(x*y), r = x - q0*b (exact with one
+// FMA), RN(q0 + r*y) = RN(x/b) while x, the quotient and r stay in the normal range.
+// Zero (x / b = x for b > 0), very small or large and non-finite x take the IEEE
+// division. Used for the gradient subtract's division by h.
+__device__ __forceinline__ float div_by(float x, float b, float y) {
+    const float ax = fabsf(x);
+    if (ax > 0x1p-100f && ax < 0x1p100f) {
+        const float q0 = __fmul_rn(x, y);
+        const float r = __fmaf_rn(-q0, b, x);
+        return __fmaf_rn(r, y, q0);
+    }
+    return ax == 0.f ? x : __fdiv_rn(x, b);
+}
+
 struct EdgeGeom {
     int i1, i2;  // block row of grid row 1 / rows - 2 (out of 0..7: none)
     int q1, q2;  // block column of grid column 1 / cols - 2 (out of 0..3: none)
@@ -386,7 +402,10 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txl = tx > 0 ? tx - 1 : 0;
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
 
-#define KREF(i) (S[no + kidx(r0 + (i), tx)])
+    // kidx(r0 + i, tx) split into a per-thread base and a compile-time row offset (r0 is a
+    // multiple of 8)
+    const int kbase = no + kidx(r0, tx);
+#define KREF(i) (S[kbase + ((i) >> 3) * (8 * RW) + ((i) & 3) * (2 * RW) + (((i) >> 2) & 1)])
 #define XREF(i) (S[co + (r0 + (i)) * RW + tx])
 
     // Row masks of this thread's column segment (bit i = row r0 + i of the region),
@@ -505,69 +524,100 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         // set_boundary_opposite_horizontal(u) / _vertical(v) (fluid_solver_gpu.cu:402-403).
         // Edge cells take the updated value of their inner neighbour (negated for the
         // normal component), corners keep their input value.
-        const float h = F.h;
+        const float h = F.h, rh = __frcp_rn(h);  // RN(1/h) for div_by
         int bad = 0;
-        // Rows go in batches of EB: first the cell each row reads u and v from (its own,
-        // or its inner neighbour's on an edge) for the whole batch, so the global loads
-        // are in flight together, then the arithmetic, in the reference's order.
-        constexpr int EB = SR;
-    #pragma unroll
-        for (int i0 = 0; i0 < SR; i0 += EB) {
-            float uin[EB], vin[EB];
-            unsigned live_rows = 0;
-    #pragma unroll
-            for (int k = 0; k < EB; ++k) {
-                const int r = r0 + i0 + k, gr = gy0 + r;
-                uin[k] = vin[k] = 0.f;
-                if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
-                const bool row_int = gr >= 1 && gr <= rows - 2;
-                int ir = gr, ic = gc;
-                if (!(col_int && row_int)) {
-                    if (row_int) ic = (gc == 0) ? 1 : cols - 2;       // left / right edge
-                    else if (col_int) ir = (gr == 0) ? 1 : rows - 2;  // top / bottom edge
+        const unsigned m_out_rows = range(H - r0, H + F.tile_h - r0) & m_in;
+        if (!edge_cta) {
+            // every output cell of an interior tile is an interior cell: u, v of all the
+            // column's output rows in flight together, then the arithmetic in the
+            // reference's order
+            float uin[SR], vin[SR];
+#pragma unroll
+            for (int i = 0; i < SR; ++i) {
+                uin[i] = vin[i] = 0.f;
+                if ((m_out_rows >> i) & 1u) {
+                    uin[i] = __ldcg(F.u_in + o0 + (size_t)i * pitch);
+                    vin[i] = __ldcg(F.v_in + o0 + (size_t)i * pitch);
                 }
-                const size_t oi = (size_t)ir * pitch + ic;
-                uin[k] = __ldcg(F.u_in + oi);
-                vin[k] = __ldcg(F.v_in + oi);
-                live_rows |= 1u << k;
             }
-    #pragma unroll
-            for (int k = 0; k < EB; ++k) {
-                if (!((live_rows >> k) & 1u)) continue;
-                const int r = r0 + i0 + k, gr = gy0 + r;
-                const bool row_int = gr >= 1 && gr <= rows - 2;
-                int ir = gr, ic = gc;
-                float su = 1.f, sv = 1.f;
-                bool corner = false;
-                if (col_int && row_int) {
-                } else if (row_int) {  // left / right edge
-                    ic = (gc == 0) ? 1 : cols - 2;
-                    su = -1.f;
-                } else if (col_int) {  // top / bottom edge
-                    ir = (gr == 0) ? 1 : rows - 2;
-                    sv = -1.f;
-                } else {
-                    corner = true;
-                }
-                const size_t o = (size_t)gr * pitch + gc;
-                float un, vn;
-                if (corner) {
-                    un = uin[k];
-                    vn = vin[k];
-                } else {
-                    const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
-                    const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
-                    const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
-                    const float gu =
-                        __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rr * RW + rcr], S[co + rr * RW + rcl])), h);
-                    const float gv =
-                        __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(S[co + rrd * RW + rc], S[co + rru * RW + rc])), h);
-                    un = su * __fsub_rn(uin[k], gu);
-                    vn = sv * __fsub_rn(vin[k], gv);
-                }
+#pragma unroll
+            for (int i = 0; i < SR; ++i) {
+                if (!((m_out_rows >> i) & 1u)) continue;
+                const int r = r0 + i;
+                const float gu =
+                    div_by(__fmul_rn(0.5f, __fsub_rn(S[co + r * RW + tx + 1], S[co + r * RW + tx - 1])), h, rh);
+                const float gv =
+                    div_by(__fmul_rn(0.5f, __fsub_rn(S[co + (r + 1) * RW + tx], S[co + (r - 1) * RW + tx])), h, rh);
+                const float un = __fsub_rn(uin[i], gu), vn = __fsub_rn(vin[i], gv);
+                const size_t o = o0 + (size_t)i * pitch;
                 F.u_out[o] = un;
                 F.v_out[o] = vn;
                 bad |= !(isfinite(un) && isfinite(vn));
+            }
+        } else {
+            // Edge tiles: rows go in batches of EB: first the cell each row reads u and v
+            // from (its own, or its inner neighbour's on an edge) for the whole batch, so
+            // the global loads are in flight together, then the arithmetic, in the
+            // reference's order.
+            constexpr int EB = 8;
+#pragma unroll
+            for (int i0 = 0; i0 < SR; i0 += EB) {
+                float uin[EB], vin[EB];
+                unsigned live_rows = 0;
+#pragma unroll
+                for (int k = 0; k < EB; ++k) {
+                    const int r = r0 + i0 + k, gr = gy0 + r;
+                    uin[k] = vin[k] = 0.f;
+                    if (r < H || r >= H + F.tile_h || gr < 0 || gr >= rows) continue;
+                    const bool row_int = gr >= 1 && gr <= rows - 2;
+                    int ir = gr, ic = gc;
+                    if (!(col_int && row_int)) {
+                        if (row_int) ic = (gc == 0) ? 1 : cols - 2;       // left / right edge
+                        else if (col_int) ir = (gr == 0) ? 1 : rows - 2;  // top / bottom edge
+                    }
+                    const size_t oi = (size_t)ir * pitch + ic;
+                    uin[k] = __ldcg(F.u_in + oi);
+                    vin[k] = __ldcg(F.v_in + oi);
+                    live_rows |= 1u << k;
+                }
+#pragma unroll
+                for (int k = 0; k < EB; ++k) {
+                    if (!((live_rows >> k) & 1u)) continue;
+                    const int r = r0 + i0 + k, gr = gy0 + r;
+                    const bool row_int = gr >= 1 && gr <= rows - 2;
+                    int ir = gr, ic = gc;
+                    float su = 1.f, sv = 1.f;
+                    bool corner = false;
+                    if (col_int && row_int) {
+                    } else if (row_int) {  // left / right edge
+                        ic = (gc == 0) ? 1 : cols - 2;
+                        su = -1.f;
+                    } else if (col_int) {  // top / bottom edge
+                        ir = (gr == 0) ? 1 : rows - 2;
+                        sv = -1.f;
+                    } else {
+                        corner = true;
+                    }
+                    const size_t o = (size_t)gr * pitch + gc;
+                    float un, vn;
+                    if (corner) {
+                        un = uin[k];
+                        vn = vin[k];
+                    } else {
+                        const int rr = min(max(ir - gy0, 0), RH - 1), rc = min(max(ic - gx0, 0), RW - 1);
+                        const int rcl = rc > 0 ? rc - 1 : 0, rcr = rc < RW - 1 ? rc + 1 : RW - 1;
+                        const int rru = rr > 0 ? rr - 1 : 0, rrd = rr < RH - 1 ? rr + 1 : RH - 1;
+                        const float gu =
+                            div_by(__fmul_rn(0.5f, __fsub_rn(S[co + rr * RW + rcr], S[co + rr * RW + rcl])), h, rh);
+                        const float gv =
+                            div_by(__fmul_rn(0.5f, __fsub_rn(S[co + rrd * RW + rc], S[co + rru * RW + rc])), h, rh);
+                        un = su * __fsub_rn(uin[k], gu);
+                        vn = sv * __fsub_rn(vin[k], gv);
+                    }
+                    F.u_out[o] = un;
+                    F.v_out[o] = vn;
+                    bad |= !(isfinite(un) && isfinite(vn));
+                }
             }
         }
         if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);

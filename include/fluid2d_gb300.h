@@ -89,6 +89,10 @@ typedef struct fs_config {
                                   convergence (read on the host after each segment). */
     int learned_cycle_iterations; /* Jacobi sweeps after each correction; 0 = 128 */
     int learned_grid;          /* coarse grid side of the network, 32 or 64; 0 = 32 */
+    int learned_defect;        /* FS_WARM_LEARNED with a residual target, steps driven from the host:
+                                  1 (default) = mixed-precision defect correction (the pressure
+                                  kept as two FP32 parts, each cycle solving for a correction of
+                                  the FP64-formed residual); 0 = corrections of the FP32 pressure */
 } fs_config;
 
 typedef struct fs_stats {
@@ -271,10 +275,10 @@ FS_API int fs_batch_sync(fs_batch* b);
 FS_API int fs_batch_get_stats(const fs_batch* b, fs_stats* out);
 FS_API int fs_batch_stream(fs_batch* b, void** stream);
 
-/* Per-kernel timing of one step. The step runs eagerly (not from the graph) in the
- * graph's shape — the same launches on the same streams, the density branch beside the
- * main stream — with a CUDA event recorded around every launch on the stream it runs
- * on. For each kernel kind: the launch count and summed event time, the part of both
+/* Per-kernel timing of one step. The step is captured in the shape of the timed graph —
+ * the same launches on the same streams, the density branch beside the main stream —
+ * with an event-record node around every launch on the stream it runs on, and replayed
+ * once (steps whose results are read on the host, learned residual solves, run eagerly). For each kernel kind: the launch count and summed event time, the part of both
  * that ran on the density branch (concurrently with the main stream, so the main
  * stream's total ms - branch_ms never exceeds the step), the algorithmic bytes of the
  * per-sweep model (each input field read once and each output written once per sweep,

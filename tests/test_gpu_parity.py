@@ -71,6 +71,10 @@ def test_project_stage(fluid, wl, rows, cols, kp, sweeps, tile_rows):
     wu, wv, _, _ = oracle.project(u, v, kp)
     assert oracle.rel_linf(gu, wu) <= 1e-6
     assert oracle.rel_linf(gv, wv) <= 1e-6
+    # no atomics and no division substitute on this path: bit for bit (the gradient's
+    # division by h is Markstein's correctly rounded quotient, checked here on every cell)
+    np.testing.assert_array_equal(gu, wu)
+    np.testing.assert_array_equal(gv, wv)
 
 
 @pytest.mark.parametrize("rows,cols", SIZES)

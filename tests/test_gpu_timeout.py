@@ -19,8 +19,8 @@ TOL = 1e-5
 
 
 def test_grid_barrier_timeout_is_reported_and_the_handle_recovers(fluid, wl):
-    w = wl.small_sources(254, seed=17)  # 256 x 256: 18 tiles, so 18 CTAs meet at each barrier
-    tol = 2e-3
+    w = wl.small_sources(128, seed=17)  # 130 x 130: 6 tiles, so 6 CTAs meet at each barrier
+    tol = 2e-2
     with fluid.Solver(w.rows, w.cols, pressure_tolerance=tol, pressure_max_iterations=20000, sweeps_per_pass=8,
                       device=0) as s:
         s.upload(*w.state())
