@@ -206,12 +206,15 @@ cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, f
 struct GsFields {
     float *d, *u, *v;
     const float *ds, *us, *vs;
-    float* scratch[4];
-    float* aux;  // two floats of device scratch
+    float* scratch[5];
+    float* aux;                 // two floats of device scratch
+    SolveCtrl* ctrl;            // grid-barrier state of the tiled solves (larger grids)
+    const unsigned* poll_limit; // device word: polls before a grid barrier gives up (0 = default)
 };
-int gs_max_size();                 // largest n on the current device
+int gs_max_size();                 // largest n of the one-CTA form on the current device (larger: tiled)
+int gs_tiled_max_size();           // largest n the method accepts
 cudaError_t gs_prepare();          // shared-memory opt-in on the current device, outside capture
 cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float diff, float visc, float dt,
-                    cudaStream_t st);
+                    cudaStream_t st, int* launches);
 
 }  // namespace fs

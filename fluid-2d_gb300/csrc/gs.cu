@@ -32,6 +32,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/fluid2d_gb300.h"
 #include "fs_internal.cuh"
 
@@ -367,6 +369,359 @@ size_t gs_smem_bytes(int n) {
     return ((size_t)n * n * sizeof(float) + 15) / 16 * 16 + kGsStage * sizeof(GsStageEntry);
 }
 
+// ---------------------------------------------------------------------------
+// Tiled form for grids larger than one SM's shared memory.
+//
+// Each in-place solve runs as one cooperative launch over kTile x kTile tiles of the
+// interior, with the field in global memory. Tile (I, J) of sweep s is processed at
+// wavefront time t = I + J + 2s, all tiles of one time in parallel, a grid barrier
+// between times. This keeps every dependency of the sequential loop: the tiles above
+// and to the left finished sweep s at time t - 1 (their new values), the tiles below
+// and to the right finished sweep s - 1 at t - 1 and start sweep s only at t + 1 (their
+// old values), and no two tiles of one time are neighbours. Inside a tile the cells are
+// updated by the same anti-diagonal wavefront as the one-CTA form, from a shared copy
+// of the tile and its one-cell halo, and an update next to a domain edge rewrites that
+// edge cell (the host solver's fill after each sweep, which only that cell reads).
+// Grid barriers wait a bounded number of polls; a CTA that gives up sets ctrl->error
+// and the solve ends early (FS_ERR_TIMEOUT on the host).
+constexpr int kTile = 64;
+constexpr int kTileThreads = 64;
+constexpr unsigned kGsBarrierPolls = 1u << 24;
+
+struct GsTiled {
+    float* x;        // field, in place (row stride P)
+    const float* c;  // constant term: x0 (diffusion) or div (pressure)
+    int n, P, iters, mode;
+    float a, den;    // diffusion
+    SolveCtrl* ctrl;
+    const unsigned* poll_limit;
+};
+
+__device__ bool gs_grid_barrier(SolveCtrl* ctrl, unsigned nblocks, unsigned limit) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &ctrl->bar_gen;
+        volatile int* err = &ctrl->error;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&ctrl->bar_count, 1u) == nblocks - 1) {
+            atomicExch(&ctrl->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctrl->bar_gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*gen == g && *err == 0) {
+                if (++spins > limit) {
+                    atomicExch(&ctrl->error, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = (*err == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <bool DIFF>
+__device__ void gs_tile(const GsTiled& S, int I, int J, float* xs, float* cs) {
+    constexpr int LD = kTile + 2;
+    const int n = S.n, P = S.P, tid = threadIdx.x, nt = blockDim.x;
+    const float s_lr = S.mode == BND_OPP_H ? -1.f : 1.f, s_tb = S.mode == BND_OPP_V ? -1.f : 1.f;
+    const int i0 = 1 + I * kTile, j0 = 1 + J * kTile;
+    const int th = min(kTile, n - 1 - i0), tw = min(kTile, n - 1 - j0);
+    for (int e = tid; e < (th + 2) * (tw + 2); e += nt) {
+        const int r = e / (tw + 2), q = e - r * (tw + 2);
+        xs[r * LD + q] = __ldcg(S.x + (size_t)(i0 - 1 + r) * P + (j0 - 1 + q));
+    }
+    for (int e = tid; e < th * tw; e += nt) {
+        const int r = e / tw, q = e - r * tw;
+        cs[r * kTile + q] = __ldcg(S.c + (size_t)(i0 + r) * P + (j0 + q));
+    }
+    __syncthreads();
+    for (int dg = 0; dg < th + tw - 1; ++dg) {
+        for (int r = tid; r < th; r += nt) {
+            const int q = dg - r;
+            if (q < 0 || q >= tw) continue;
+            const int o = (r + 1) * LD + q + 1;
+            float val;
+            if (DIFF) {  // (x0 + a*(U + D + L + R)) / (1 + 4a), fluid_solver_cpu.cpp:107-108
+                float sum = __fadd_rn(xs[o - LD], xs[o + LD]);
+                sum = __fadd_rn(sum, xs[o - 1]);
+                sum = __fadd_rn(sum, xs[o + 1]);
+                val = __fdiv_rn(__fadd_rn(cs[r * kTile + q], __fmul_rn(S.a, sum)), S.den);
+            } else {     // (div + R + L + D + U) / 4, fluid_solver_cpu.cpp:199-200
+                float sum = __fadd_rn(cs[r * kTile + q], xs[o + 1]);
+                sum = __fadd_rn(sum, xs[o - 1]);
+                sum = __fadd_rn(sum, xs[o + LD]);
+                sum = __fadd_rn(sum, xs[o - LD]);
+                val = __fdiv_rn(sum, 4.0f);
+            }
+            xs[o] = val;
+            const int gi = i0 + r, gj = j0 + q;
+            if (gj == 1) xs[o - 1] = s_lr * val;
+            if (gj == n - 2) xs[o + 1] = s_lr * val;
+            if (gi == 1) xs[o - LD] = s_tb * val;
+            if (gi == n - 2) xs[o + LD] = s_tb * val;
+        }
+        __syncthreads();
+    }
+    // the tile, and the domain-edge cells next to it (the other halo cells belong to
+    // other tiles)
+    for (int e = tid; e < th * tw; e += nt) {
+        const int r = e / tw, q = e - r * tw;
+        S.x[(size_t)(i0 + r) * P + (j0 + q)] = xs[(r + 1) * LD + q + 1];
+    }
+    for (int q = tid; q < tw; q += nt) {
+        if (i0 == 1) S.x[j0 + q] = xs[q + 1];
+        if (i0 + th == n - 1) S.x[(size_t)(n - 1) * P + j0 + q] = xs[(th + 1) * LD + q + 1];
+    }
+    for (int r = tid; r < th; r += nt) {
+        if (j0 == 1) S.x[(size_t)(i0 + r) * P] = xs[(r + 1) * LD];
+        if (j0 + tw == n - 1) S.x[(size_t)(i0 + r) * P + n - 1] = xs[(r + 1) * LD + tw + 1];
+    }
+    __syncthreads();  // xs is reused by this CTA's next tile
+}
+
+template <bool DIFF>
+__global__ void __launch_bounds__(kTileThreads) gs_tiled_kernel(const __grid_constant__ GsTiled S) {
+    __shared__ float xs[(kTile + 2) * (kTile + 2)];
+    __shared__ float cs[kTile * kTile];
+    const int m = S.n - 2, NT = (m + kTile - 1) / kTile, K = S.iters;
+    const unsigned G = gridDim.x;
+    const unsigned lim_set = S.poll_limit ? __ldcg(S.poll_limit) : 0u;
+    const unsigned limit = lim_set ? lim_set : kGsBarrierPolls;
+    const int last_t = 2 * (NT - 1) + 2 * (K - 1);
+    for (int t = 0; t <= last_t; ++t) {
+        int base = 0;
+        for (int s = max(0, (t - 2 * (NT - 1) + 1) / 2); s <= min(K - 1, t / 2); ++s) {
+            const int d = t - 2 * s;
+            const int ilo = max(0, d - NT + 1), ihi = min(NT - 1, d);
+            for (int k = 0; k <= ihi - ilo; ++k)
+                if ((unsigned)(base + k) % G == blockIdx.x) gs_tile<DIFF>(S, ilo + k, d - ilo - k, xs, cs);
+            base += max(0, ihi - ilo + 1);
+        }
+        if (t < last_t && !gs_grid_barrier(S.ctrl, G, limit)) return;
+    }
+}
+
+// The host solver's fill (cpu_fill) on a field in global memory, one CTA.
+__global__ void __launch_bounds__(kGsThreads) gs_fill_kernel(float* g, int n, int P, int mode) { cpu_fill(g, n, P, mode); }
+
+// x += dt*s on the interior and x0 = x (the diffusion's constant term).
+__global__ void gs_add_copy_kernel(float* x, const float* __restrict__ src, float* __restrict__ x0, int n, int P,
+                                   float dt) {
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const size_t o = (size_t)i * P + j;
+        float val = x[o];
+        if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+            val = __fadd_rn(val, __fmul_rn(dt, src[o]));
+            x[o] = val;
+        }
+        x0[o] = val;
+    }
+}
+
+// su = u, sv = v and the largest interior displacement |dt0 * velocity| into dmax[0..1]
+// (float bits, non-negative, so an integer maximum orders them; zeroed before).
+__global__ void gs_copy_vel_kernel(const GsArgs A) {
+    const int n = A.n, P = A.P;
+    float dm = 0.f;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const size_t o = (size_t)i * P + j;
+        const float u = A.f[1][o], v = A.f[2][o];
+        A.su[o] = u;
+        A.sv[o] = v;
+        if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+            float a = fmaxf(fabsf(__fmul_rn(A.dt0, u)), fabsf(__fmul_rn(A.dt0, v)));
+            if (!(a <= 1e30f)) a = 1e30f;
+            dm = fmaxf(dm, a);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(A.dmax), __float_as_int(dm));
+}
+
+// Divergence (fluid_solver_cpu.cpp:186-191) into dv and p = 0.
+__global__ void gs_div_kernel(const GsArgs A, float* p) {
+    const int n = A.n, P = A.P;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)n * n; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const size_t o = (size_t)i * P + j;
+        p[o] = 0.f;
+        if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+            const float* u = A.f[1];
+            const float* v = A.f[2];
+            float s = __fsub_rn(u[o + 1], u[o - 1]);
+            s = __fadd_rn(s, v[o + P]);
+            s = __fsub_rn(s, v[o - P]);
+            A.dv[o] = __fmul_rn(__fmul_rn(-0.5f, A.h), s);
+        }
+    }
+}
+
+// remove_p (fluid_solver_cpu.cpp:205-210) on the interior.
+__global__ void gs_remove_p_kernel(const GsArgs A, const float* __restrict__ p) {
+    const int n = A.n, P = A.P, m = n - 2;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)m * m; e += (long)gridDim.x * blockDim.x) {
+        const size_t o = (size_t)(1 + e / m) * P + 1 + e % m;
+        float* u = A.f[1];
+        float* v = A.f[2];
+        u[o] = __fsub_rn(u[o], __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(p[o + 1], p[o - 1])), A.h));
+        v[o] = __fsub_rn(v[o], __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(p[o + P], p[o - P])), A.h));
+    }
+}
+
+// advect(trace=false) of u and v by the copies (su, sv) on the interior
+// (fluid_solver_cpu.cpp:154-173).
+__global__ void gs_gather_grid_kernel(const GsArgs A) {
+    const int n = A.n, P = A.P, m = n - 2;
+    const float hi = (float)n - 1.5f;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)m * m; e += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(e / m), j = 1 + (int)(e % m);
+        const size_t o = (size_t)i * P + j;
+        float x = __fsub_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
+        float y = __fsub_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
+        x = (x < hi) ? x : hi;
+        x = (1.5f < x) ? x : 1.5f;
+        y = (y < hi) ? y : hi;
+        y = (1.5f < y) ? y : 1.5f;
+        const int j0 = (int)x, i0 = (int)y;
+        const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+        const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+        const size_t a = (size_t)i0 * P + j0;
+        for (int k = 0; k < 2; ++k) {
+            const float* g0 = k == 0 ? A.su : A.sv;
+            const float top = __fadd_rn(__fmul_rn(s1, g0[a]), __fmul_rn(s0, g0[a + 1]));
+            const float bot = __fadd_rn(__fmul_rn(s1, g0[a + P]), __fmul_rn(s0, g0[a + P + 1]));
+            A.f[1 + k][o] = __fadd_rn(__fmul_rn(s3, top), __fmul_rn(s2, bot));
+        }
+    }
+}
+
+// The splat by target (gs_splat_gather) over every target block; when some source
+// moves more than kGatherMaxDTiled cells, one CTA applies the contributions in the raster
+// order of their sources into the global accumulator instead.
+constexpr int kGatherMaxDTiled = 40;
+__global__ void __launch_bounds__(kGsThreads) gs_splat_grid_kernel(const GsArgs A) {
+    const float dm = fmaxf(__ldcg(A.dmax), __ldcg(A.dmax + 1));
+    if (dm <= (float)kGatherMaxDTiled) {
+        gs_splat_gather(A, blockIdx.x, (int)ceilf(dm));
+        return;
+    }
+    if (blockIdx.x != 0) return;
+    const int n = A.n, P = A.P, m = n - 2;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) A.acc[(size_t)(1 + e / m) * P + 1 + e % m] = 0.f;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const float hi = (float)n - 1.5f;
+    for (int i = 1; i < n - 1; ++i)
+        for (int j = 1; j < n - 1; ++j) {
+            const size_t o = (size_t)i * P + j;
+            const float x = __fadd_rn((float)j, __fmul_rn(A.dt0, A.su[o]));
+            const float y = __fadd_rn((float)i, __fmul_rn(A.dt0, A.sv[o]));
+            if (!(x >= 0.5f && x <= hi && y >= 0.5f && y <= hi)) continue;
+            const int j0 = (int)x, i0 = (int)y;
+            const float s0 = __fsub_rn(x, (float)j0), s1 = __fsub_rn(1.f, s0);
+            const float s2 = __fsub_rn(y, (float)i0), s3 = __fsub_rn(1.f, s2);
+            const float w = A.f[0][o];
+            float* t = A.acc + (size_t)i0 * P + j0;
+            // the accumulator's edge cells are never read back (the density takes its
+            // interior, then the fill), so every target can be added to
+            t[0] = __fadd_rn(t[0], __fmul_rn(__fmul_rn(s1, s3), w));
+            t[P] = __fadd_rn(t[P], __fmul_rn(__fmul_rn(s1, s2), w));
+            t[1] = __fadd_rn(t[1], __fmul_rn(__fmul_rn(s0, s3), w));
+            t[P + 1] = __fadd_rn(t[P + 1], __fmul_rn(__fmul_rn(s0, s2), w));
+        }
+}
+
+// d = the splat result on the interior (the fill follows).
+__global__ void gs_take_acc_kernel(const GsArgs A) {
+    const int n = A.n, P = A.P, m = n - 2;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < (long)m * m; e += (long)gridDim.x * blockDim.x) {
+        const size_t o = (size_t)(1 + e / m) * P + 1 + e % m;
+        A.f[0][o] = A.acc[o];
+    }
+}
+
+int g_tiled_blocks[64] = {};  // co-resident CTAs of gs_tiled_kernel per device (set-up)
+
+cudaError_t gs_solve_tiled(const GsTiled& S, bool diff, cudaStream_t st) {
+    if (S.iters <= 0) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int m = S.n - 2, NT = (m + kTile - 1) / kTile;
+    const int want = NT * std::min(NT, S.iters);  // most tiles of one wavefront time
+    const int blocks = std::max(1, std::min(g_tiled_blocks[dev & 63], want));
+    e = cudaMemsetAsync(S.ctrl, 0, sizeof(SolveCtrl), st);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kTileThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return diff ? cudaLaunchKernelEx(&cfg, gs_tiled_kernel<true>, S) : cudaLaunchKernelEx(&cfg, gs_tiled_kernel<false>, S);
+}
+
+int grid_blocks(long work, int threads) { return (int)std::max<long>(1, std::min<long>((work + threads - 1) / threads, 4096)); }
+
+// A step of the host solver's method on a grid too large for the one-CTA form: the
+// same order of operations (fluid_solver_cpu.cpp:6-31), each solve a tiled cooperative
+// launch, the rest grid-wide kernels.
+cudaError_t gs_step_tiled(const GsFields& F, const GsArgs& A, cudaStream_t st) {
+    const int n = A.n, P = A.P;
+    const long cells = (long)n * n;
+    const int B = grid_blocks(cells, 256);
+    const int modes[3] = {BND_CONT, BND_OPP_H, BND_OPP_V};
+    float* x0 = F.scratch[2];  // the divergence's buffer doubles as the diffusion's x0
+    float* p = F.scratch[4];
+    cudaError_t e = cudaMemsetAsync(A.dmax, 0, 2 * sizeof(float), st);
+    if (e != cudaSuccess) return e;
+    gs_copy_vel_kernel<<<B, 256, 0, st>>>(A);
+    auto diffuse = [&](int k) -> cudaError_t {
+        gs_add_copy_kernel<<<B, 256, 0, st>>>(A.f[k], A.src[k], x0, n, P, A.dt);
+        GsTiled S{A.f[k], x0, n, P, A.kd, modes[k], A.a[k], A.den[k], F.ctrl, F.poll_limit};
+        cudaError_t r = gs_solve_tiled(S, true, st);
+        if (r == cudaSuccess && A.kd > 0) gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[k], n, P, modes[k]);
+        return r == cudaSuccess ? cudaGetLastError() : r;
+    };
+    auto project = [&]() -> cudaError_t {
+        gs_div_kernel<<<B, 256, 0, st>>>(A, p);
+        GsTiled S{p, A.dv, n, P, A.kp, BND_CONT, 0.f, 0.f, F.ctrl, F.poll_limit};
+        cudaError_t r = gs_solve_tiled(S, false, st);
+        if (r != cudaSuccess) return r;
+        if (A.kp > 0) gs_fill_kernel<<<1, kGsThreads, 0, st>>>(p, n, P, BND_CONT);
+        gs_remove_p_kernel<<<B, 256, 0, st>>>(A, p);
+        gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[1], n, P, BND_OPP_H);
+        gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[2], n, P, BND_OPP_V);
+        return cudaGetLastError();
+    };
+    if ((e = diffuse(0)) != cudaSuccess) return e;
+    const int target_blocks = (int)(((long)(n - 2) * (n - 2) + kGsThreads - 1) / kGsThreads);
+    gs_splat_grid_kernel<<<target_blocks, kGsThreads, 0, st>>>(A);
+    gs_take_acc_kernel<<<B, 256, 0, st>>>(A);
+    gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[0], n, P, BND_CONT);
+    if ((e = diffuse(1)) != cudaSuccess) return e;
+    if ((e = diffuse(2)) != cudaSuccess) return e;
+    if ((e = project()) != cudaSuccess) return e;
+    gs_copy_vel_kernel<<<B, 256, 0, st>>>(A);  // copies for the velocity advection
+    gs_gather_grid_kernel<<<B, 256, 0, st>>>(A);
+    gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[1], n, P, BND_OPP_H);
+    gs_fill_kernel<<<1, kGsThreads, 0, st>>>(A.f[2], n, P, BND_OPP_V);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return project();
+}
+
 }  // namespace
 
 int gs_max_size() {
@@ -378,10 +733,24 @@ int gs_max_size() {
     return n;
 }
 
+int gs_tiled_max_size() { return 16384; }
+
 cudaError_t gs_prepare() {
     // the largest size, so that handles of different sizes share one setting
     const int n = gs_max_size();
     if (n < 3) return cudaErrorNoDevice;
+    {
+        int dev = 0, sms = 0, per = 0;
+        cudaError_t r = cudaGetDevice(&dev);
+        if (r == cudaSuccess) r = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (r == cudaSuccess)
+            r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gs_tiled_kernel<true>, kTileThreads, 0);
+        int per2 = 0;
+        if (r == cudaSuccess)
+            r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, gs_tiled_kernel<false>, kTileThreads, 0);
+        if (r != cudaSuccess) return r;
+        g_tiled_blocks[dev & 63] = std::min(per, per2) * sms;
+    }
     const int bytes = (int)gs_smem_bytes(n);
     cudaError_t e = cudaFuncSetAttribute(gs_diffuse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
@@ -392,7 +761,7 @@ cudaError_t gs_prepare() {
 }
 
 cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float diff, float visc, float dt,
-                    cudaStream_t st) {
+                    cudaStream_t st, int* launches) {
     GsArgs A;
     A.f[0] = F.d;
     A.f[1] = F.u;
@@ -420,6 +789,11 @@ cudaError_t gs_step(const GsFields& F, int n, int pitch, int kd, int kp, float d
     A.dt = dt;
     A.dt0 = sqrtf(cells) * dt;
     A.h = 1.0f / sqrtf(cells);
+    if (n > gs_max_size()) {
+        *launches = 29;
+        return gs_step_tiled(F, A, st);
+    }
+    *launches = 4;
     const size_t smem = gs_smem_bytes(n);
     gs_diffuse_kernel<<<3, kGsThreads, smem, st>>>(A);
     const int target_blocks = ((n - 2) * (n - 2) + kGsThreads - 1) / kGsThreads;

@@ -682,7 +682,8 @@ int enqueue_project_learned_defect(fs_solver* s, const float* u_in, const float*
         CK(cudaMemsetAsync(s->ecur, 0, fbytes, s->stream));
         CK(cudaMemsetAsync(P.ctrl, 0, sizeof(SolveCtrl), s->stream));
         if ((rc = enqueue_network_correction(s, s->rhs, s->ecur, nullptr, cnt)) != FS_OK) return rc;
-        const int budget = std::min(per, cap - used);
+        // the last cycle gets the rest of the cap, as in the FP32 form
+        const int budget = c + 1 < cycles ? std::min(per, cap - used) : cap - used;
         P.max_passes = std::max(1, (budget + K - 1) / K);
         P.tol = (float)std::min(0.5, hsums[0] > 0.0 ? tol * std::sqrt(hsums[1] / hsums[0]) : 1.0);
         PROF_BEGIN(s);
@@ -909,10 +910,14 @@ int enqueue_step(fs_solver* s, float diff, float visc, float dt, Counter& cnt) {
         F.vs = s->src[F_V];
         for (int k = 0; k < 3; ++k) F.scratch[k] = s->x0[k];
         F.scratch[3] = s->acc;
+        F.scratch[4] = s->p[0];
         F.aux = s->div;  // unused by this method
+        F.ctrl = s->ctrl;
+        F.poll_limit = reinterpret_cast<const unsigned*>(s->flags + 1);
+        int launches = 0;
         CK(gs_step(F, s->rows, s->pitch, s->cfg.diffuse_iterations, s->cfg.pressure_iterations, diff, visc, dt,
-                   s->stream));
-        cnt.launches += 4;
+                   s->stream, &launches));
+        cnt.launches += launches;
         return FS_OK;
     }
     if (!s->density_branch) {
@@ -1028,6 +1033,15 @@ int check_flags(fs_solver* s) {
             return fail(FS_ERR_TIMEOUT, "learned correction: a tensor-core wait gave up; the network is disabled "
                                         "until fs_set_network");
         }
+    }
+    // the tiled Gauss-Seidel solves' grid barriers (control block 0), once per step
+    if (s->cfg.method == FS_METHOD_GAUSS_SEIDEL && s->rows > gs_max_size() && s->stats.steps > 0 &&
+        s->steps_reported != s->stats.steps) {
+        s->steps_reported = s->stats.steps;
+        SolveCtrl c[2];
+        int rc = read_solve_ctrl(s, c);
+        if (rc != FS_OK) return rc;
+        if (c[0].error) return fail(FS_ERR_TIMEOUT, "Gauss-Seidel solve: a grid barrier timed out");
     }
     // the residual solves' outcome is reported once per step: later syncs without a new
     // step do not report it again
@@ -1212,7 +1226,7 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
     s->sweeps = cfg->sweeps_per_pass > 0 ? std::min(cfg->sweeps_per_pass, maxk) : default_sweeps(cfg, dev, maxk);
     s->density_branch = density_branch_pays(s, dev);
 
-    if (cfg->method == FS_METHOD_GAUSS_SEIDEL && cfg->rows > gs_max_size()) {
+    if (cfg->method == FS_METHOD_GAUSS_SEIDEL && cfg->rows > gs_tiled_max_size()) {
         delete s;
         return fail(FS_ERR_ARG, "fs_create: grid too large for the Gauss-Seidel method (fs_gauss_seidel_max_size)");
     }
@@ -1343,7 +1357,7 @@ int fs_create(const fs_config* cfg, fs_solver** out) {
 
 int fs_gauss_seidel_max_size(int* n) {
     if (!n) return fail(FS_ERR_ARG, "fs_gauss_seidel_max_size: null argument");
-    *n = gs_max_size();
+    *n = gs_max_size() > 0 ? gs_tiled_max_size() : 0;
     return *n > 0 ? FS_OK : fail(FS_ERR_CUDA, "fs_gauss_seidel_max_size: no CUDA device");
 }
 

@@ -116,6 +116,8 @@ __device__ __forceinline__ int kidx(int r, int c) {
 // FMA), RN(q0 + r*y) = RN(x/b) while x, the quotient and r stay in the normal range.
 // Zero (x / b = x for b > 0), very small or large and non-finite x take the IEEE
 // division. Used for the gradient subtract's division by h.
+__device__ __noinline__ float ieee_div(float x, float b) { return __fdiv_rn(x, b); }
+
 __device__ __forceinline__ float div_by(float x, float b, float y) {
     const float ax = fabsf(x);
     if (ax > 0x1p-100f && ax < 0x1p100f) {
@@ -123,7 +125,7 @@ __device__ __forceinline__ float div_by(float x, float b, float y) {
         const float r = __fmaf_rn(-q0, b, x);
         return __fmaf_rn(r, y, q0);
     }
-    return ax == 0.f ? x : __fdiv_rn(x, b);
+    return ax == 0.f ? x : ieee_div(x, b);  // out of line: rare, and keeps the epilogue small
 }
 
 struct EdgeGeom {
@@ -459,7 +461,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     } else if (kind == PASS_DIFFUSE_FIRST) {
         // add_sources_kernel (fluid_solver_gpu.cu:64) fused into the load
         const float dt = F.dt;
-#pragma unroll
+#pragma unroll 8
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
             float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
@@ -468,7 +470,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             KREF(i) = x;
         }
     } else {
-#pragma unroll
+#pragma unroll 8
         for (int i = 0; i < SR; ++i) {
             const size_t o = o0 + (size_t)i * pitch;
             S[co + (r0 + i) * RW + tx] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
@@ -507,12 +509,12 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         float* __restrict__ y = yout;
         float* __restrict__ ko = F.cst_out;
         if (y) {
-#pragma unroll
+#pragma unroll 8
             for (int i = 0; i < SR; ++i)
                 if ((m_out >> i) & 1u) y[o0 + (size_t)i * pitch] = XREF(i);
         }
         if (ko) {
-#pragma unroll
+#pragma unroll 8
             for (int i = 0; i < SR; ++i)
                 if ((m_out >> i) & 1u) ko[o0 + (size_t)i * pitch] = KREF(i);
         }
@@ -528,31 +530,34 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
         int bad = 0;
         const unsigned m_out_rows = range(H - r0, H + F.tile_h - r0) & m_in;
         if (!edge_cta) {
-            // every output cell of an interior tile is an interior cell: u, v of all the
-            // column's output rows in flight together, then the arithmetic in the
-            // reference's order
-            float uin[SR], vin[SR];
+            // every output cell of an interior tile is an interior cell: batches of eight
+            // rows, the batch's u and v loads in flight together, then the arithmetic in
+            // the reference's order
+#pragma unroll 1
+            for (int i0 = 0; i0 < SR; i0 += 8) {
+                float uin[8], vin[8];
 #pragma unroll
-            for (int i = 0; i < SR; ++i) {
-                uin[i] = vin[i] = 0.f;
-                if ((m_out_rows >> i) & 1u) {
-                    uin[i] = __ldcg(F.u_in + o0 + (size_t)i * pitch);
-                    vin[i] = __ldcg(F.v_in + o0 + (size_t)i * pitch);
+                for (int k = 0; k < 8; ++k) {
+                    uin[k] = vin[k] = 0.f;
+                    if ((m_out_rows >> (i0 + k)) & 1u) {
+                        uin[k] = __ldcg(F.u_in + o0 + (size_t)(i0 + k) * pitch);
+                        vin[k] = __ldcg(F.v_in + o0 + (size_t)(i0 + k) * pitch);
+                    }
                 }
-            }
 #pragma unroll
-            for (int i = 0; i < SR; ++i) {
-                if (!((m_out_rows >> i) & 1u)) continue;
-                const int r = r0 + i;
-                const float gu =
-                    div_by(__fmul_rn(0.5f, __fsub_rn(S[co + r * RW + tx + 1], S[co + r * RW + tx - 1])), h, rh);
-                const float gv =
-                    div_by(__fmul_rn(0.5f, __fsub_rn(S[co + (r + 1) * RW + tx], S[co + (r - 1) * RW + tx])), h, rh);
-                const float un = __fsub_rn(uin[i], gu), vn = __fsub_rn(vin[i], gv);
-                const size_t o = o0 + (size_t)i * pitch;
-                F.u_out[o] = un;
-                F.v_out[o] = vn;
-                bad |= !(isfinite(un) && isfinite(vn));
+                for (int k = 0; k < 8; ++k) {
+                    if (!((m_out_rows >> (i0 + k)) & 1u)) continue;
+                    const int r = r0 + i0 + k;
+                    const float gu =
+                        div_by(__fmul_rn(0.5f, __fsub_rn(S[co + r * RW + tx + 1], S[co + r * RW + tx - 1])), h, rh);
+                    const float gv = div_by(
+                        __fmul_rn(0.5f, __fsub_rn(S[co + (r + 1) * RW + tx], S[co + (r - 1) * RW + tx])), h, rh);
+                    const float un = __fsub_rn(uin[k], gu), vn = __fsub_rn(vin[k], gv);
+                    const size_t o = o0 + (size_t)(i0 + k) * pitch;
+                    F.u_out[o] = un;
+                    F.v_out[o] = vn;
+                    bad |= !(isfinite(un) && isfinite(vn));
+                }
             }
         } else {
             // Edge tiles: rows go in batches of EB: first the cell each row reads u and v
@@ -560,7 +565,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
             // the global loads are in flight together, then the arithmetic, in the
             // reference's order.
             constexpr int EB = 8;
-#pragma unroll
+#pragma unroll 1
             for (int i0 = 0; i0 < SR; i0 += EB) {
                 float uin[EB], vin[EB];
                 unsigned live_rows = 0;
@@ -627,7 +632,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // ||div + sum(nbrs) - 4p||^2 and ||div||^2 over this tile's interior output
     // cells, from the final p (valid one ring beyond the tile: halo = sweeps + 1).
     if (resid && col_out) {
-#pragma unroll
+#pragma unroll 8
         for (int i = 0; i < SR; ++i) {
             const int r = r0 + i, gr = gy0 + r;
             if (r < H || r >= H + F.tile_h || !col_int || gr < 1 || gr > rows - 2) continue;

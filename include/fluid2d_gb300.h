@@ -131,8 +131,9 @@ FS_API int fs_config_init(fs_config* cfg, int rows, int cols);
 FS_API int fs_create(const fs_config* cfg, fs_solver** out);
 
 /* Largest grid side (rows = cols, boundary included) that FS_METHOD_GAUSS_SEIDEL accepts
- * on the calling thread's current device: one field must fit in one SM's shared memory.
- * Writes 0 when no device is usable. */
+ * on the calling thread's current device (16384). Grids whose field fits one SM's shared
+ * memory (234 a side on a GB300) run each solve in one CTA; larger ones run it as a tiled
+ * wavefront over the whole GPU. Writes 0 when no device is usable. */
 FS_API int fs_gauss_seidel_max_size(int* n);
 
 /* Device-resident simulation driver: the reference's simulation::add_*_source and

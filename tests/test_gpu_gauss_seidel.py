@@ -2,8 +2,10 @@
 fluid_solver_cpu (src/fluid_solver_cpu.cpp:6-215) reproduced on the GPU, bit for bit.
 
 Checked against the golden fixtures written by the compiled reference itself, and against
-the oracle's restatement of the host solver on seeded workloads, sizes from 3 to the
-largest grid the method accepts, and iteration counts other than the reference's 20/20."""
+the oracle's restatement of the host solver (pinned bit for bit to the compiled host
+solver) on seeded workloads: sizes from 3 to the largest one-CTA grid (234 on a GB300),
+the tiled form above it (235, 301, the reference app's 800 and the benchmark's 2050),
+iteration counts other than the reference's 20/20, and both splat paths."""
 import pathlib
 
 import numpy as np
@@ -62,17 +64,63 @@ def test_sizes_and_iteration_counts(fluid, wl, n, kd, kp):
         np.testing.assert_array_equal(g_, o)
 
 
-def test_largest_grid(fluid, wl):
-    n = fluid.gauss_seidel_max_size()
-    assert n >= 200
+ONE_CTA_MAX = 234  # the largest grid whose field fits one GB300 SM's shared memory
+
+
+def _vs_oracle(fluid, n, d, u, v, ds, us, vs, diff, visc, dt, steps, kd=20, kp=20):
+    with _gs(fluid, n, diffuse_iterations=kd, pressure_iterations=kp) as s:
+        s.upload(d, u, v)
+        s.upload_sources(ds, us, vs)
+        s.step(diff, visc, dt, steps)
+        got = s.download()
+    want = oracle.cpu_solve(d, ds, diff, u, v, us, vs, visc, dt, kd=kd, kp=kp, nsteps=steps)
+    for g_, o in zip(got, want):
+        np.testing.assert_array_equal(g_, o)
+
+
+@pytest.mark.parametrize("n", [ONE_CTA_MAX, ONE_CTA_MAX + 1])
+def test_either_side_of_the_one_cta_limit(fluid, wl, n):
     w = wl.small_sources(n - 2, seed=5)
+    _vs_oracle(fluid, n, w.d, w.u, w.v, w.ds, w.us, w.vs, w.diffusion, w.viscosity, w.dt, 4)
+
+
+@pytest.mark.parametrize("n,kd,kp,vmax", [(301, 20, 20, 0.5), (301, 7, 33, 0.5), (257, 0, 5, 0.5), (300, 20, 20, 2.0)])
+def test_tiled_sizes_counts_and_splat_paths(fluid, wl, n, kd, kp, vmax):
+    """vmax 2.0 moves sources ~60 cells: the in-order splat; 0.5 the gathering one."""
+    d, u, v, ds, us, vs = wl.random_state(n, n, n + kd, vmax=vmax)
+    _vs_oracle(fluid, n, d, u, v, ds, us, vs, 0.05, 0.02, 0.1, 3, kd, kp)
+
+
+def test_reference_app_size(fluid, wl):
+    """800 x 800, the reference app's grid (src/app.cpp:30-31), vortex field, 20/20, 5 steps."""
+    w = wl.vortex_field(798, seed=6, kd=20, kp=20, vortices=24, rmin=8, rmax=30)
+    _vs_oracle(fluid, w.rows, w.d, w.u, w.v, w.ds, w.us, w.vs, w.diffusion, w.viscosity, w.dt, 5)
+
+
+def test_benchmark_size(fluid, wl):
+    """2050 x 2050, the benchmark's vortex field at the host solver's 20/20, 2 steps."""
+    w = wl.vortex_field(2048, seed=2, kd=20, kp=20)
+    _vs_oracle(fluid, w.rows, w.d, w.u, w.v, w.ds, w.us, w.vs, w.diffusion, w.viscosity, w.dt, 2)
+
+
+def test_tiled_barrier_timeout(fluid, wl):
+    """A tiled solve whose grid-barrier waits run out after one poll reports
+    FS_ERR_TIMEOUT; with the default bound restored the same handle steps exactly."""
+    n = 301
+    d, u, v, ds, us, vs = wl.random_state(n, n, 3, vmax=0.5)
     with _gs(fluid, n) as s:
-        s.upload(w.d, w.u, w.v)
-        s.upload_sources(w.ds, w.us, w.vs)
-        s.step(w.diffusion, w.viscosity, w.dt, 4)
-        gd, gu, gv = s.download()
-    od, ou, ov = oracle.cpu_solve(w.d, w.ds, w.diffusion, w.u, w.v, w.us, w.vs, w.viscosity, w.dt, nsteps=4)
-    for g_, o in ((gd, od), (gu, ou), (gv, ov)):
+        s.upload(d, u, v)
+        s.upload_sources(ds, us, vs)
+        s.set_barrier_poll_limit(1)
+        with pytest.raises(fluid.FluidError) as e:
+            s.step(0.05, 0.02, 0.1)
+        assert e.value.code == fluid.FS_ERR_TIMEOUT
+        s.set_barrier_poll_limit(0)
+        s.upload(d, u, v)
+        s.step(0.05, 0.02, 0.1)
+        got = s.download()
+    want = oracle.cpu_solve(d, ds, 0.05, u, v, us, vs, 0.02, 0.1, nsteps=1)
+    for g_, o in zip(got, want):
         np.testing.assert_array_equal(g_, o)
 
 
