@@ -19,8 +19,9 @@ inline __host__ __device__ float bnd_sign_lr(int m) { return m == BND_OPP_H ? -1
 inline __host__ __device__ float bnd_sign_tb(int m) { return m == BND_OPP_V ? -1.f : 1.f; }
 
 // Stencil pass kinds. A diffusion or pressure solve is split into passes; each pass
-// loads a tile with a halo, runs `sweeps` Jacobi sweeps in shared memory and writes
-// the tile back once (temporal blocking).
+// loads a tile with a halo, runs `sweeps` Jacobi sweeps on chip (registers, with
+// shuffles and a shared-memory row exchange) and writes the tile back once (temporal
+// blocking).
 enum PassKind : int {
     PASS_DIFFUSE_FIRST = 0,  // x0 = x + dt*s fused in (add_sources); writes x0
     PASS_DIFFUSE = 1,        // reads x, x0
@@ -28,7 +29,8 @@ enum PassKind : int {
     PASS_PRESSURE = 3,       // reads p, div
 };
 
-// Region width of the stencil kernels: one column per thread, four warps across.
+// Region width of the stencil kernels: 128 columns, one per thread of a CTA row in the
+// load and store phases, four per lane of a warp in the sweeps.
 constexpr int kRegionW = 128;
 
 struct StencilField {
