@@ -78,6 +78,8 @@ def parse():
                     help="sweep cap per projection (default: residual 2000, learned 20000, depth 400)")
     ap.add_argument("--count", type=int, default=256)
     ap.add_argument("--gs-size", type=int, default=128, help="gauss-seidel: interior cells per side")
+    ap.add_argument("--depth-target-steps", type=int, default=0,
+                    help="depth: also time coarse-corrected solves that reach --tol, for this many steps")
     ap.add_argument("--tune", action="store_true", help="autotune the tiling before timing")
     ap.add_argument("--cycles", type=int, default=0, help="learned: most corrections per projection (0 = cap / cycle-iters)")
     ap.add_argument("--cycle-iters", type=int, default=128, help="learned: Jacobi sweeps after each correction")
@@ -478,9 +480,13 @@ def run_small(a):
     s.upload_sources(*w.sources())
     stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
     s.step(w.diffusion, w.viscosity, w.dt, nsteps=a.warmup)
+    clocks = ClockSampler(0)
+    clocks.start()
     ms = _timed_steps(lambda: s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False), s.sync, stream, a.steps,
                       lambda: None, torch, 0)
+    clk = clocks.stop()
     line = {"metric": metric_name(), "value": w.interior_cells * a.steps / (ms / 1e3), "unit": "cell-steps/s",
+            "clocks": clk,
             "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded sources)",
             "config": {"workload": "small_sources 128x128 interior, 20/20 sweeps, dt 0.1, rates 1e-4",
@@ -491,10 +497,14 @@ def run_small(a):
 
 
 def run_depth(a):
-    """Temporal-blocking depth on a large grid: the vortex field with the pressure solve
-    run to a relative-residual target under an iteration cap (the cap binds, so every
-    depth does the same sweeps), at depth 1 (one sweep per HBM pass, the plain kernels)
-    and depths 2, 4, 8 and the tuned default; reports ms/step and the sweeps done."""
+    """Temporal-blocking depth on a large grid (8192^2 vortex field, pressure to a
+    relative-residual target, 50 steps): plain Jacobi from the previous pressure under a
+    sweep cap (the cap binds: Jacobi damps the smooth modes at ~pi^2/N^2 per sweep, so
+    1e-4 is out of its reach at this size and every depth does the same sweeps) at depth
+    1 (one sweep per HBM pass, the plain kernels), 2, 4, 8, the default and the
+    autotuner's choice; then, with --depth-target-steps, the same target reached by
+    coarse-corrected Jacobi cycles (the learned warm start's machinery with an all-zero
+    network and the FP64 defect correction) at depth 1 and at the tuned depth."""
     import torch
 
     pkg = __graft_entry__.load_package()
@@ -502,16 +512,25 @@ def run_depth(a):
 
     build_lib.build()
     w = workloads.vortex_field(a.size, seed=2, kd=a.kd, kp=a.kp)
-    out = []
-    for depth in (1, 2, 4, 8, 0):
-        cfg = dict(diffuse_iterations=a.kd, pressure_tolerance=a.tol, pressure_max_iterations=a.max_iters,
-                   warm_start=pkg.FS_WARM_PREVIOUS, device=0, check_finite=0, sweeps_per_pass=depth)
+    base = dict(diffuse_iterations=a.kd, pressure_tolerance=a.tol, warm_start=pkg.FS_WARM_PREVIOUS, device=0,
+                check_finite=0)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    tuned = pkg.autotune(w.rows, w.cols, w.diffusion, w.viscosity, w.dt, steps=2,
+                         pressure_max_iterations=a.max_iters, **base)
+    tuned["tuning_s"] = time.perf_counter() - t0
+    print(json.dumps({"autotuner": tuned}), flush=True)
+
+    def run(cfg, steps, net=None):
         s = pkg.Solver(w.rows, w.cols, **cfg)
+        if net is not None:
+            s.set_network(net)
         s.upload(*w.state())
         s.upload_sources(*w.sources())
         stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
         sweeps, res, ms_tot = [], [], 0.0
-        for k in range(a.warmup + a.steps):
+        for k in range(a.warmup + steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False)
@@ -526,19 +545,42 @@ def run_depth(a):
                 ms_tot += e0.elapsed_time(e1)
                 sweeps += st["pressure_iterations_last"]
                 res += st["pressure_residual_last"]
-        ms = ms_tot / a.steps
+        s.close()
+        return st, ms_tot / steps, sweeps, res
+
+    out = []
+    plans = [(d, 0, str(d)) for d in (1, 2, 4, 8)] + [(0, 0, "default"),
+                                                      (tuned["sweeps_per_pass"], tuned["tile_rows"], "autotuned")]
+    for depth, rows_, name in plans:
+        cfg = dict(base, pressure_max_iterations=a.max_iters, sweeps_per_pass=depth, tile_rows=rows_)
+        st, ms, sweeps, res = run(cfg, a.steps)
         total_sweeps = 3 * a.kd + float(np.mean(sweeps)) * 2
-        out.append({"depth": st["sweeps_per_pass"], "requested": depth or "default", "ms_per_step": ms,
-                    "pressure_sweeps_per_projection": float(np.mean(sweeps)), "residual_max": float(np.max(res)),
+        out.append({"depth": st["sweeps_per_pass"], "tile_rows": st["tile_rows"], "requested": name,
+                    "ms_per_step": ms, "pressure_sweeps_per_projection": float(np.mean(sweeps)),
+                    "residual_max": float(np.max(res)),
                     "cell_sweeps_per_s": w.interior_cells * total_sweeps / (ms / 1e3)})
         print(json.dumps(out[-1]), flush=True)
-        s.close()
+    target = []
+    if a.depth_target_steps > 0:
+        from fluid2d_gb300 import learned
+
+        zero_net = np.zeros(learned.NPARAM, np.float32)
+        for depth, rows_, name in ((1, 0, "1"), (tuned["sweeps_per_pass"], tuned["tile_rows"], "autotuned")):
+            cfg = dict(base, warm_start=pkg.FS_WARM_LEARNED, pressure_max_iterations=20000,
+                       sweeps_per_pass=depth, tile_rows=rows_)
+            st, ms, sweeps, res = run(cfg, a.depth_target_steps, zero_net)
+            target.append({"depth": st["sweeps_per_pass"], "tile_rows": st["tile_rows"], "requested": name,
+                           "ms_per_step": ms, "pressure_sweeps_per_projection": float(np.mean(sweeps)),
+                           "residual_max": float(np.max(res)),
+                           "missed_target": int(np.sum(np.array(res) > a.tol)), "steps": a.depth_target_steps})
+            print(json.dumps(target[-1]), flush=True)
     line = {"metric": "ms/step by temporal-blocking depth", "unit": "ms/step", "higher_is_better": False,
             "value": out[-1]["ms_per_step"], "steps": a.steps, "warmup": a.warmup, "dtype": "f32",
             "data": "synthetic (seeded vortex field)",
             "config": {"workload": f"vortex_field {a.size}^2, Kd={a.kd}, pressure to {a.tol:g} relative residual, "
                                    f"cap {a.max_iters} sweeps (binding)", "l2": "inputs far larger than L2"},
-            "depths": out}
+            "autotuner": tuned, "depths": out, "to_target_coarse_corrected": target,
+            "clocks": clocks.stop()}
     print(json.dumps(line), flush=True)
 
 
@@ -561,17 +603,22 @@ def run_gauss_seidel(a):
     if N <= 128:
         w = workloads.small_sources(N, seed=1)
         desc = f"small_sources {N}x{N} interior, Gauss-Seidel 20/20 sweeps, dt 0.1, rates 1e-4"
+        data = "synthetic (seeded sources)"
     else:
         w = workloads.vortex_field(N, seed=2, kd=20, kp=20)
         desc = f"vortex_field {N}x{N} interior, Gauss-Seidel 20/20 sweeps, dt 0.05, rates 1e-5"
+        data = "synthetic (seeded vortex field)"
     steps = a.steps
     s = pkg.FluidSolverGaussSeidel(w.rows, device=0, check_finite=0)
     s.upload(*w.state())
     s.upload_sources(*w.sources())
     stream = torch.cuda.ExternalStream(s.device_view().stream, device=0)
     s.step(w.diffusion, w.viscosity, w.dt, nsteps=a.warmup)
+    clocks = ClockSampler(0)
+    clocks.start()
     ms = _timed_steps(lambda: s.step(w.diffusion, w.viscosity, w.dt, 1, sync=False), s.sync, stream, steps,
                       lambda: None, torch, 0)
+    clk = clocks.stop()
     gd, gu, gv = s.download()
     od, ou, ov = w.state()
     od, ou, ov = oracle.cpu_solve(od, w.ds, w.diffusion, ou, ov, w.us, w.vs, w.viscosity, w.dt,
@@ -600,7 +647,7 @@ def run_gauss_seidel(a):
     line = {"metric": f"cell-steps/s, Gauss-Seidel method (the reference's host solver), {w.rows}^2",
             "value": cells * steps / (ms / 1e3), "unit": "cell-steps/s", "n_gpus": 1, "steps": steps,
             "warmup": a.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic (seeded sources)", "bit_exact_vs_oracle": exact,
+            "data": data, "bit_exact_vs_oracle": exact, "clocks": clk,
             "e2e": {"value": cells * steps / e2e_s, "unit": "cell-steps/s",
                     "h2d_bytes_per_step": 6 * w.rows * w.cols * 4, "d2h_bytes_per_step": 3 * w.rows * w.cols * 4},
             "cpu_baseline": {"value": cells * cpu_steps / cpu_s, "unit": "cell-steps/s", "cores": 1, "kind": "port",
@@ -722,6 +769,8 @@ def run_residual(a):
 
     build_lib.build()
     w = workloads.vortex_field(a.size, seed=2, kd=a.kd, kp=a.kp)
+    clocks = ClockSampler(0)
+    clocks.start()
     out = []
     for warm in (0, 1):
         cfg = dict(diffuse_iterations=a.kd, pressure_tolerance=a.tol, pressure_max_iterations=a.max_iters,
@@ -760,7 +809,7 @@ def run_residual(a):
             "data": "synthetic (seeded vortex field)",
             "config": {"workload": f"vortex_field {a.size}^2, pressure to {a.tol:g} relative residual, "
                                    f"cap {a.max_iters} sweeps, Kd={a.kd}"},
-            "modes": out}
+            "modes": out, "clocks": clocks.stop()}
     print(json.dumps(line), flush=True)
 
 
@@ -813,6 +862,8 @@ def run_learned(a):
             np.save(a.weights, params)
         del X1, T1, X2, T2, sets
         torch.cuda.empty_cache()
+    clocks = ClockSampler(0)
+    clocks.start()
     results = []
     for size in [int(x) for x in a.eval_sizes.split(",")]:
         w = workloads.vortex_field(size, seed=3, kd=a.kd, kp=a.kp)
@@ -866,6 +917,7 @@ def run_learned(a):
     line = {"metric": "ms/step to relative pressure residual, learned vs previous-pressure warm start",
             "unit": "ms/step", "higher_is_better": False, "steps": a.steps, "warmup": a.warmup, "dtype": "f32",
             "data": "synthetic (seeded vortex fields)", "training": info, "results": results,
+            "clocks": clocks.stop(),
             "config": {"workload": f"vortex_field {a.eval_sizes}, Kd={a.kd}, cap {a.max_iters} sweeps",
                        "network": "8 conv layers 3x3x32, BF16 tcgen05 implicit GEMM, 32x32 coarse grid",
                        "cycles": a.cycles, "cycle_iterations": a.cycle_iters}}

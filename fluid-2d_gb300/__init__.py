@@ -120,6 +120,9 @@ SIGNATURES = {
     "fs_net_upsample2_bwd": (C.c_int, [_P, _P, _I, _I, _P]),
     "fs_net_relu_bwd": (C.c_int, [_P, _P, _P, _P, _P, C.c_longlong, _I, _P]),
     "fs_net_weight_grad": (C.c_int, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "fs_net_weight_grad_tc_work_floats": (C.c_longlong, [_I, _I]),
+    "fs_net_infer32": (C.c_int, [_P, _P, _P, _P, _P, _I, _P, _P]),
+    "fs_net_weight_grad_tc": (C.c_int, [_P, _P, _P, _P, _P, C.c_longlong, _I, _I, _I, _I, _P, _P]),
     "fs_net_flip_weights": (C.c_int, [_P, _P, _P]),
     "fs_net_mse": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P]),
     "fs_net_adam": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _F, _F, _F, _F, _I, _P, _P]),

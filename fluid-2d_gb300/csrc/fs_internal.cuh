@@ -153,6 +153,10 @@ cudaError_t conv_prepare();
 int conv3x3_launch(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip, void* y,
                    float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores, int* err,
                    const int* skip_if, void* stream);
+// The whole network on `images` 32 x 32 grids, one launch (fs_net_infer32), with the
+// same skip flag.
+int net_infer32_launch(const void* x0, const void* wpk, const float* params, void* e1, float* y, int images,
+                       int* err, const int* skip_if, void* stream);
 
 // Learned corrections (net.cu). Coarse residual: block sums of the residual of p (null =
 // zero) into bs[G*G], their squared norm into *norm2 and, when xin is given, the network

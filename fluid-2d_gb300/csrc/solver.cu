@@ -448,18 +448,26 @@ int enqueue_network_correction(fs_solver* s, const float* rhs, float* p_cur, con
                               out >= 0 ? net_act(s, out) : nullptr, yf, g, g, g, up, relu, 1, s->net.err, converged,
                               s->stream);
     };
-    // e1 (G) -> pool -> e2, e3 (G/2) -> pool -> b1, b2 (G/4) -> d1 (+e3) -> d2 (+e1) -> out
-    if ((rc = conv(0, 0, 1, 0, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = fs_net_avgpool2(net_act(s, 1), net_act(s, 2), G / 2, G / 2, s->stream)) != FS_OK) return rc;
-    if ((rc = conv(1, 2, 3, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = conv(2, 3, 4, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = fs_net_avgpool2(net_act(s, 4), net_act(s, 5), G / 4, G / 4, s->stream)) != FS_OK) return rc;
-    if ((rc = conv(3, 5, 6, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = conv(4, 6, 7, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = conv(5, 7, 8, 1, 1, 4, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = conv(6, 8, 9, 0, 1, 1, 1, nullptr)) != FS_OK) return rc;
-    if ((rc = conv(7, 9, 10, 0, 0, -1, 0, s->net.y)) != FS_OK) return rc;
-    cnt.launches += 10;
+    // e1 (G) -> pool -> e2, e3 (G/2) -> pool -> b1, b2 (G/4) -> d1 (+e3) -> d2 (+e1) -> out:
+    // one fused launch on the 32 x 32 grid, layer by layer on the 64 x 64 one
+    if (G == 32) {
+        if ((rc = net_infer32_launch(net_act(s, 0), s->net.wpk, s->net.params, net_act(s, 1), s->net.y, 1, s->net.err,
+                                     converged, s->stream)) != FS_OK)
+            return rc;
+        cnt.launches += 1;
+    } else {
+        if ((rc = conv(0, 0, 1, 0, 0, -1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = fs_net_avgpool2(net_act(s, 1), net_act(s, 2), G / 2, G / 2, s->stream)) != FS_OK) return rc;
+        if ((rc = conv(1, 2, 3, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = conv(2, 3, 4, 1, 0, -1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = fs_net_avgpool2(net_act(s, 4), net_act(s, 5), G / 4, G / 4, s->stream)) != FS_OK) return rc;
+        if ((rc = conv(3, 5, 6, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = conv(4, 6, 7, 2, 0, -1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = conv(5, 7, 8, 1, 1, 4, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = conv(6, 8, 9, 0, 1, 1, 1, nullptr)) != FS_OK) return rc;
+        if ((rc = conv(7, 9, 10, 0, 0, -1, 0, s->net.y)) != FS_OK) return rc;
+        cnt.launches += 10;
+    }
     // candidate A: the network's correction, post-smoothed; B: the coarse smoothing alone
     float* pb = s->p[1];  // free between pressure passes
     CK(launch_coarse_smooth(s->net.y, s->net.y, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
@@ -779,8 +787,16 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
 int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out, int slot,
                     Counter& cnt) {
     if (s->cfg.pressure_tolerance > 0.f) return enqueue_project_to_residual(s, u_in, v_in, u_out, v_out, slot, cnt);
-    const std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
+    std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
     const int m = (int)plan.size();
+    // The last pass needs one ring more than its sweeps for the gradient. When that would
+    // make its halo one more than a multiple of four, it gives one sweep to the first
+    // pass: its halo then matches the middle passes' and its interior tiles take the
+    // direct path (16-byte aligned regions). The sweeps run in the same order either way.
+    if (m >= 2 && plan[m - 1] >= 1 && plan[m - 1] % 4 == 0 && plan[0] + 1 <= stencil_max_halo(s->tile_rows) - 1) {
+        plan[0] += 1;
+        plan[m - 1] -= 1;
+    }
     const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
     const float* pin = nullptr;

@@ -16,8 +16,11 @@
 // The sweeps are register-blocked (run_sweeps): each thread holds an 8 x 4 block of
 // the field in registers, exchanges block edges with its neighbours by warp shuffles
 // and a small shared-memory row exchange, and reads its constant terms (x0 or div) from
-// shared memory, one barrier per sweep. Loads, stores and the fused first/last-pass
-// arithmetic use a one-column-per-thread layout for coalesced global access. The
+// shared memory, one barrier per sweep. Interior tiles of the diffusion passes and the
+// middle pressure passes load and store the block layout straight from global memory
+// (16-byte accesses); edge tiles and the first and last pressure passes stage the
+// region in shared memory in a one-column-per-thread layout, where the masked loads,
+// the fused divergence and the gradient epilogue run. The
 // reference's per-sweep boundary fill is folded into the sweep (the cells next to a
 // domain edge read what the fill would have stored there) and applied for real once,
 // after the last sweep. Arithmetic follows the reference's operand order with explicit
@@ -319,35 +322,167 @@ __device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi,
     }
 }
 
+// Interior tiles of the passes without an epilogue (diffusion passes, middle pressure
+// passes) need neither the column layout nor any masking: the region lies inside the
+// grid's interior, so every cell is loaded and every cell is live. There the field and
+// its constant term go straight from global memory into the block layout (a lane's four
+// columns of a row are one 16-byte load, a warp's row 512 contiguous bytes), and the
+// final field straight back from registers, without staging the region in shared
+// memory ("direct" tiles). Requires the region's first column and the row pitch to be
+// multiples of four floats and the buffers 16-byte aligned (checked by the caller).
 struct SweepParams {
     int nsweeps, edge, gy0, gx0, rows, cols;
     float s_lr, s_tb, a, dh, dl, rf;
+    // direct tiles only
+    int direct;
+    const float* x;  // field in
+    const float* k;  // constant term in (x0 / div), or the source s of a first diffusion pass
+    float* y;        // field out (output tile; may be null)
+    float* kout;     // first diffusion pass: x0 out (output tile; may be null)
+    int pitch, halo, tile_h, tile_w, first;
+    float dt;
+    const StencilField* F;  // last pressure pass: the gradient epilogue's fields (else null)
 };
 
-// The sweeps of one tile in the block layout of run_sweeps: the field goes from shared
-// memory (row-major at xoff) into registers, the sweeps run (constant terms read at koff
-// in the kidx layout, the exchange area overlaying the field's buffer), and the final
-// field goes back to xoff. Kept out of line so that the tile body's other live values
-// are saved once around the call instead of competing with the register blocks.
-template <bool DIFF, int NW>
+// Stores the four values v of one block row (columns cb .. cb+3 of the region) where
+// they fall in the output columns [c_lo, c_hi) (relative to cb).
+__device__ __forceinline__ void store_row4(float* p, float4 v, int c_lo, int c_hi) {
+    if (c_lo <= 0 && c_hi >= 4) {
+        *reinterpret_cast<float4*>(p) = v;
+    } else {
+        if (c_lo <= 0 && c_hi > 0) p[0] = v.x;
+        if (c_lo <= 1 && c_hi > 1) p[1] = v.y;
+        if (c_lo <= 2 && c_hi > 2) p[2] = v.z;
+        if (c_lo <= 3 && c_hi > 3) p[3] = v.w;
+    }
+}
+
+// Gradient subtract of a direct tile of the last pressure pass (remove_p_kernel,
+// fluid_solver_gpu.cu:202-203): u -= (0.5*(pR - pL))/h, v -= (0.5*(pD - pU))/h on the
+// output cells, from the final pressure block in registers. Left/right neighbours of the
+// block's edge columns come by shuffles, the rows above and below by one more row
+// exchange, in the buffer the last sweep did not use (`eoff`). Interior tiles only: no
+// reflecting fill is needed.
+template <int NW>
+__device__ __forceinline__ void gradient_direct(const float2 (&X)[4][4], int eoff, int w, int lane, size_t o,
+                                                size_t pitch, int r_lo, int r_hi, int c_lo, int c_hi,
+                                                const StencilField& F) {
+    constexpr int RW = kRegionW;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ float4 smem4[];
+    float* const E = reinterpret_cast<float*>(smem4) + eoff;
+    const int my_top = (2 * w) * RW + 4 * lane, my_bot = my_top + RW;
+    const int nb_up = w > 0 ? my_top - RW : my_top;
+    const int nb_dn = w < NW - 1 ? my_top + 2 * RW : my_bot;
+    *reinterpret_cast<float4*>(E + my_top) = make_float4(X[0][0].x, X[0][1].x, X[0][2].x, X[0][3].x);
+    *reinterpret_cast<float4*>(E + my_bot) = make_float4(X[3][0].y, X[3][1].y, X[3][2].y, X[3][3].y);
+    __syncthreads();
+    const float4 u4 = *reinterpret_cast<const float4*>(E + nb_up);
+    const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn);
+    const float up[4] = {u4.x, u4.y, u4.z, u4.w}, dn[4] = {d4.x, d4.y, d4.z, d4.w};
+    const float h = F.h, rh = __frcp_rn(h);
+    const bool out_cols = c_lo < 4 && c_hi > 0;
+    int bad = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        auto pv = [&](int ii, int q) -> float { return (ii >> 2) ? X[ii & 3][q].y : X[ii & 3][q].x; };
+        const float L0 = __shfl_up_sync(FULL, pv(i, 3), 1);
+        const float R3 = __shfl_down_sync(FULL, pv(i, 0), 1);
+        if (i < r_lo || i >= r_hi || !out_cols) continue;
+        const float4 ui = __ldcg(reinterpret_cast<const float4*>(F.u_in + o + i * pitch));
+        const float4 vi = __ldcg(reinterpret_cast<const float4*>(F.v_in + o + i * pitch));
+        const float uin[4] = {ui.x, ui.y, ui.z, ui.w}, vin[4] = {vi.x, vi.y, vi.z, vi.w};
+        float un[4], vn[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float pl = q > 0 ? pv(i, q - 1) : L0;
+            const float pr = q < 3 ? pv(i, q + 1) : R3;
+            const float pu = i > 0 ? pv(i - 1, q) : up[q];
+            const float pd = i < 7 ? pv(i + 1, q) : dn[q];
+            const float gu = div_by(__fmul_rn(0.5f, __fsub_rn(pr, pl)), h, rh);
+            const float gv = div_by(__fmul_rn(0.5f, __fsub_rn(pd, pu)), h, rh);
+            un[q] = __fsub_rn(uin[q], gu);
+            vn[q] = __fsub_rn(vin[q], gv);
+            if (q >= c_lo && q < c_hi) bad |= !(isfinite(un[q]) && isfinite(vn[q]));
+        }
+        store_row4(F.u_out + o + i * pitch, make_float4(un[0], un[1], un[2], un[3]), c_lo, c_hi);
+        store_row4(F.v_out + o + i * pitch, make_float4(vn[0], vn[1], vn[2], vn[3]), c_lo, c_hi);
+    }
+    if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
+}
+
+// The sweeps of one tile in the block layout of run_sweeps. Staged tiles: the field
+// comes from shared memory (row-major at xoff) and goes back there; direct tiles: from
+// and to global memory, the constant terms written to shared memory here. The sweeps
+// read the constant terms at koff in the kidx layout, the exchange area overlaying the
+// field's buffer. Kept out of line so that the tile body's other live values are saved
+// once around the call instead of competing with the register blocks, and so that
+// staged and direct interior tiles share one copy of the sweep loop.
+// MODE: 0 staged tiles only, 1 also direct tiles, 2 also the direct gradient epilogue.
+template <bool DIFF, int NW, int MODE>
 __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P) {
     constexpr int RW = kRegionW;
     extern __shared__ float4 smem4[];
-    float* const X = reinterpret_cast<float*>(smem4) + xoff;
+    float* const S = reinterpret_cast<float*>(smem4);
+    float* const X = S + xoff;
     const int tid = threadIdx.y * RW + threadIdx.x;
     const int w = tid >> 5, lane = tid & 31;
     const int rb = w * 8, cb = 4 * lane;
+    const size_t pitch = (size_t)P.pitch;
+    const size_t o = (size_t)(P.gy0 + rb) * pitch + (size_t)(P.gx0 + cb);
+    // direct tiles: output rows [r_lo, r_hi) and columns [c_lo, c_hi) relative to this
+    // thread's block
+    const int r_lo = P.halo - rb, r_hi = P.halo + P.tile_h - rb;
+    const int c_lo = P.halo - cb, c_hi = P.halo + P.tile_w - cb;
+    const bool out_cols = c_lo < 4 && c_hi > 0;
     float2 xb[4][4];
+    if (MODE > 0 && P.direct) {
+        float* const K = S + koff + w * (8 * RW) + 4 * lane;
+        float4 t[8], kk[8];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const float4 t = *reinterpret_cast<const float4*>(X + (rb + j) * RW + cb);
-        const float4 b = *reinterpret_cast<const float4*>(X + (rb + j + 4) * RW + cb);
-        xb[j][0] = make_float2(t.x, b.x);
-        xb[j][1] = make_float2(t.y, b.y);
-        xb[j][2] = make_float2(t.z, b.z);
-        xb[j][3] = make_float2(t.w, b.w);
+        for (int i = 0; i < 8; ++i) t[i] = __ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch));
+#pragma unroll
+        for (int i = 0; i < 8; ++i) kk[i] = __ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch));
+        if (P.first) {
+            // add_sources_kernel (fluid_solver_gpu.cu:64), fused as compiled: x0 = x + dt*s
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                t[i].x = __fmaf_rn(P.dt, kk[i].x, t[i].x);
+                t[i].y = __fmaf_rn(P.dt, kk[i].y, t[i].y);
+                t[i].z = __fmaf_rn(P.dt, kk[i].z, t[i].z);
+                t[i].w = __fmaf_rn(P.dt, kk[i].w, t[i].w);
+                kk[i] = t[i];
+            }
+            if (P.kout != nullptr && out_cols) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (i >= r_lo && i < r_hi) store_row4(P.kout + o + i * pitch, kk[i], c_lo, c_hi);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            xb[j][0] = make_float2(t[j].x, t[j + 4].x);
+            xb[j][1] = make_float2(t[j].y, t[j + 4].y);
+            xb[j][2] = make_float2(t[j].z, t[j + 4].z);
+            xb[j][3] = make_float2(t[j].w, t[j + 4].w);
+            // kidx layout: (row j, row j+4) of columns (0, 1), then of columns (2, 3); each
+            // thread reads back only the constant terms it wrote
+            *reinterpret_cast<float4*>(K + j * (2 * RW)) = make_float4(kk[j].x, kk[j + 4].x, kk[j].y, kk[j + 4].y);
+            *reinterpret_cast<float4*>(K + j * (2 * RW) + RW) =
+                make_float4(kk[j].z, kk[j + 4].z, kk[j].w, kk[j + 4].w);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 t = *reinterpret_cast<const float4*>(X + (rb + j) * RW + cb);
+            const float4 b = *reinterpret_cast<const float4*>(X + (rb + j + 4) * RW + cb);
+            xb[j][0] = make_float2(t.x, b.x);
+            xb[j][1] = make_float2(t.y, b.y);
+            xb[j][2] = make_float2(t.z, b.z);
+            xb[j][3] = make_float2(t.w, b.w);
+        }
+        __syncthreads();  // the exchange area of the sweeps overlays the field's buffer
     }
-    __syncthreads();  // the exchange area of the sweeps overlays the field's buffer
     const Coef2 c = {make_float2(P.a, P.a), make_float2(-P.dh, -P.dh), make_float2(-P.dl, -P.dl),
                      make_float2(P.rf, P.rf)};
     if (P.edge) {
@@ -357,6 +492,21 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
     } else {
         const EdgeGeom g = {-1, -1, -1, -1, P.s_lr, P.s_tb};
         run_sweeps<DIFF, false, NW>(xb, koff, xoff, P.nsweeps, w, lane, g, c);
+    }
+    if (MODE > 0 && P.direct) {
+        if (P.y != nullptr && out_cols) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (i < r_lo || i >= r_hi) continue;
+                const int j = i & 3;
+                const float4 v = (i < 4) ? make_float4(xb[j][0].x, xb[j][1].x, xb[j][2].x, xb[j][3].x)
+                                         : make_float4(xb[j][0].y, xb[j][1].y, xb[j][2].y, xb[j][3].y);
+                store_row4(P.y + o + i * pitch, v, c_lo, c_hi);
+            }
+        }
+        if (MODE > 1 && P.F != nullptr) gradient_direct<NW>(xb, xoff + (P.nsweeps & 1) * (2 * NW * RW), w, lane, o, pitch, r_lo,
+                                                r_hi, c_lo, c_hi, *P.F);
+        return;  // the next tile's first barrier orders the exchange area's reuse
     }
     __syncthreads();  // every warp has read its last exchange rows
 #pragma unroll
@@ -375,7 +525,8 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
 // output tile, then the optional gradient-subtract epilogue and the optional residual
 // partial sums (for residual-driven pressure solves). xin/yout stand in for F.x/F.y so
 // a persistent caller can ping-pong buffers across passes.
-template <int TY, int SRB, bool DIFF>
+// MODE as for sweep_phase.
+template <int TY, int SRB, bool DIFF, int MODE = 2>
 __device__ __forceinline__ void process_tile(const StencilField& F, int b, const float* __restrict__ xin,
                                              float* __restrict__ yout, bool resid,
                                              float& rnum, float& rden) {
@@ -403,6 +554,32 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const bool col_int = gc >= 1 && gc <= cols - 2;
     const int txl = tx > 0 ? tx - 1 : 0;
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
+    const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
+
+    if (MODE > 0 && !edge_cta && !resid && kind != PASS_PRESSURE_FIRST && F.sweeps > 0 && (MODE > 1 || !F.epilogue) &&
+        (((gx0 | F.pitch) & 3) == 0) &&
+        ((reinterpret_cast<uintptr_t>(xin) | reinterpret_cast<uintptr_t>(F.x2) |
+          reinterpret_cast<uintptr_t>(F.cst) | reinterpret_cast<uintptr_t>(yout) |
+          reinterpret_cast<uintptr_t>(F.cst_out) | reinterpret_cast<uintptr_t>(F.u_in) |
+          reinterpret_cast<uintptr_t>(F.v_in) | reinterpret_cast<uintptr_t>(F.u_out) |
+          reinterpret_cast<uintptr_t>(F.v_out)) & 15) == 0) {
+        const bool first = kind == PASS_DIFFUSE_FIRST;
+        SweepParams P = {F.sweeps, 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        P.direct = 1;
+        P.x = xin;
+        P.k = first ? F.x2 : F.cst;
+        P.y = yout;
+        P.kout = first ? F.cst_out : nullptr;
+        P.pitch = F.pitch;
+        P.halo = H;
+        P.tile_h = F.tile_h;
+        P.tile_w = F.tile_w;
+        P.first = first ? 1 : 0;
+        P.dt = F.dt;
+        P.F = (!DIFF && F.epilogue) ? &F : nullptr;
+        sweep_phase<DIFF, NW, MODE>(0, RH * RW, P);
+        return;
+    }
 
     // kidx(r0 + i, tx) split into a per-thread base and a compile-time row offset (r0 is a
     // multiple of 8)
@@ -480,10 +657,11 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
-    const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
     if (F.sweeps > 0) {
-        const SweepParams P = {F.sweeps, edge_cta ? 1 : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
-        sweep_phase<DIFF, NW>(co, no, P);
+        SweepParams P = {F.sweeps, edge_cta ? 1 : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        P.direct = 0;
+        P.F = nullptr;
+        sweep_phase<DIFF, NW, MODE>(co, no, P);
         if (edge_cta) {
             fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
             // restore_corners: the reference never writes the four corners; the sweeps
@@ -758,7 +936,9 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 template <int TY, int SRB>
 __device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, bool resid,
                                            float& rn, float& rd) {
-    process_tile<TY, SRB, false>(F, t, x, y, resid, rn, rd);
+    // staged tiles only: the passes of a residual solve need the staged layout for the
+    // residual sums, and the direct paths' extra live values would spill in this call chain
+    process_tile<TY, SRB, false, 0>(F, t, x, y, resid, rn, rd);
 }
 
 template <int TY, int SRB>

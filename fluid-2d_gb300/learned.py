@@ -171,11 +171,16 @@ class Net:
         return self.y
 
     # ------------------------------------------------------------- backward
-    def backward(self, x0, dy, stream=None):
-        """Gradient of the loss w.r.t. all parameters (FP32 [NPARAM]) given dL/dy."""
+    def backward(self, x0, dy, stream=None, tensor_cores=True):
+        """Gradient of the loss w.r.t. all parameters (FP32 [NPARAM]) given dL/dy. With
+        tensor_cores the weight gradients run as tcgen05 implicit GEMMs over the pixels
+        (BF16 dz), otherwise on CUDA cores (FP32 dz, the checked reference)."""
         torch = self.torch
         L = _lib()
         a = self.act
+        if tensor_cores and getattr(self, "wg_work", None) is None:
+            self.wg_work = torch.empty(int(L.fs_net_weight_grad_tc_work_floats(0, 0)), dtype=torch.float32,
+                                       device=self.dev)
         grad = torch.zeros(NPARAM, dtype=torch.float32, device=self.dev)
         gw = lambda li: grad[li * NPARAM_LAYER: li * NPARAM_LAYER + CH * 9 * CH]
         gb = lambda li: grad[li * NPARAM_LAYER + CH * 9 * CH: (li + 1) * NPARAM_LAYER]
@@ -192,8 +197,13 @@ class Net:
             dz = torch.empty((r, c, CH), dtype=torch.float32, device=self.dev)
             dzb = torch.empty((r, c, CH), dtype=torch.bfloat16, device=self.dev)
             _chk(L.fs_net_relu_bwd(_p(da), _p(da2), _p(out_act), _p(dz), _p(dzb), n, int(relu), stream))
-            _chk(L.fs_net_weight_grad(_p(dz), _p(x_in), _p(gw(li)), _p(gb(li)), r, c, self.g >> lvl_out, int(up),
-                                      stream))
+            if tensor_cores:
+                _chk(L.fs_net_weight_grad_tc(_p(dzb), _p(x_in), _p(gw(li)), _p(gb(li)), _p(self.wg_work),
+                                             self.wg_work.numel(), r, c, self.g >> lvl_out, int(up), _p(self.err),
+                                             stream))
+            else:
+                _chk(L.fs_net_weight_grad(_p(dz), _p(x_in), _p(gw(li)), _p(gb(li)), r, c, self.g >> lvl_out,
+                                          int(up), stream))
             if not want_dx:
                 return None, dz
             dxh = torch.empty((r, c, CH), dtype=torch.float32, device=self.dev)

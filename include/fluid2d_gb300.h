@@ -250,7 +250,9 @@ FS_API int fs_checkpoint_load(fs_solver* s, const char* path);
 FS_API int fs_stage(fs_solver* s, int stage, float rate, float dt);
 
 /* Autotuner: times whole steps of candidate stencil tilings (region height 64/128 x
- * blocking depth 4..16) for cfg's grid and sweep plan on the device and writes the
+ * blocking depth 2..16) for cfg's grid and sweep plan on the device (on a smooth
+ * velocity field with divergence everywhere, so that residual-target solves do real
+ * work) and writes the
  * fastest into cfg->tile_rows / cfg->sweeps_per_pass. With a cache_path the choice is
  * looked up first and stored after tuning (key: device, SM count, rows, cols, kd, kp,
  * tolerance, warm start). No counterpart in the reference (fixed 32x32 launches,
@@ -320,8 +322,8 @@ FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, 
  * Scratch (divergence and two pressure buffers) lives in a fixed file-scope device
  * array of 3 x FS_NOALLOC_MAX_CELLS floats (12 MiB) that every GPU loading this library
  * holds until process exit; rows * pitch above FS_NOALLOC_MAX_CELLS is rejected with
- * FS_ERR_ARG. The first call on a device looks up that array's address and caches it:
- * make it before any stream capture. After cudaDeviceReset() on a device the cached
+ * FS_ERR_ARG. The first call on a device looks up that array's address and caches it.
+ * After cudaDeviceReset() on a device the cached
  * address is stale and further calls on that device are not supported. All calls share
  * the array, so calls that may overlap on the GPU race and must be serialised by the
  * caller. */
@@ -338,6 +340,14 @@ FS_API int fs_project_noalloc(const float* u, const float* v, float* u_out, floa
  * ([co][tap][ci], 32 x 9 x 32). All pointers are device pointers; `err` (nullable) is
  * set if a tensor-core wait gave up. */
 FS_API int fs_conv_pack_weights(const float* w32, void* wpk, void* stream);
+/* The whole 8-layer network of the learned warm start on `images` 32 x 32 grids in one
+ * launch (one CTA per grid, activations in shared memory, every conv on tcgen05):
+ * x0 (images x 32 x 32 x 32 BF16 NHWC), wpk (8 x 9216 packed weights, fs_conv_pack_weights
+ * of each layer), params (the FP32 parameters, 8 x 9248: weights then 32 biases per
+ * layer), e1 (scratch of x0's size), y (FP32 output, images x 32 x 32 x 32). Same
+ * results as the layer-by-layer fs_conv3x3 sequence. */
+FS_API int fs_net_infer32(const void* x0, const void* wpk, const float* params, void* e1, float* y, int images,
+                          int* err, void* stream);
 FS_API int fs_conv3x3(const void* x, const void* wpk, const float* w32, const float* bias, const void* skip,
                       void* y, float* yf, int H, int W, int img_h, int up, int relu, int use_tensor_cores,
                       int* err, void* stream);
@@ -361,6 +371,14 @@ FS_API int fs_net_relu_bwd(const float* da, const float* da2, const void* a, flo
                            int relu, void* stream);
 FS_API int fs_net_weight_grad(const float* dz, const void* x, float* dw, float* db, int H, int W, int img_h, int up,
                               void* stream);
+/* The weight gradient on the tensor cores: dw += sum_p dz x im2col(x) and db += sum_p dz
+ * from the BF16 copy dzb of dz, as a tcgen05 implicit GEMM over the pixels (FP32
+ * accumulation in tensor memory), per-CTA partial sums in `work` (work_floats floats;
+ * fs_net_weight_grad_tc_work_floats() is enough for any size on the current device)
+ * and a fixed-order reduction, so the result is deterministic. `err` as in fs_conv3x3. */
+FS_API long long fs_net_weight_grad_tc_work_floats(int H, int W);
+FS_API int fs_net_weight_grad_tc(const void* dzb, const void* x, float* dw, float* db, float* work,
+                                 long long work_floats, int H, int W, int img_h, int up, int* err, void* stream);
 FS_API int fs_net_flip_weights(const float* w, float* wt, void* stream);
 FS_API int fs_net_mse(const float* y, const float* target, float* dy, float* loss_part, long long n, void* stream);
 FS_API int fs_net_adam(float* w, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,

@@ -61,6 +61,36 @@ def test_forward_and_gradients_match_cpu_reference(fluid):
     assert np.all(grad[~live] == 0.0)
 
 
+def test_fused_inference_matches_layer_by_layer(fluid):
+    """fs_net_infer32 (the whole network in one launch, activations in shared memory)
+    gives the same output as the eight per-layer tensor-core convolutions and two pools."""
+    import ctypes as C
+
+    import torch
+
+    Lm, _ = _mods()
+    G, B = Lm.G, 3
+    rng = np.random.default_rng(5)
+    params = Lm.init_params(4)
+    params += (rng.standard_normal(params.size) * 0.05).astype(np.float32) * (1 - Lm.frozen_mask())
+    x0 = np.zeros((B, G, G, 32), np.float32)
+    x0[..., :2] = rng.standard_normal((B, G, G, 2))
+    dev = torch.device("cuda", 0)
+    net = Lm.Net(B=B, params=torch.from_numpy(params).to(dev))
+    xg = torch.from_numpy(x0).to(torch.bfloat16).to(dev).reshape(B * G, G, 32)
+    want = net.forward(xg).clone()
+    e1 = torch.empty_like(xg)
+    got = torch.full_like(want, float("nan"))
+    L = fluid.load()
+    p = lambda t: C.c_void_p(t.data_ptr())
+    assert L.fs_net_infer32(p(xg), p(net.wpk), p(net.params), p(e1), p(got), B, p(net.err), None) == 0
+    torch.cuda.synchronize()
+    assert int(net.err.item()) == 0
+    w, g = want.cpu().numpy(), got.cpu().numpy()
+    assert np.isfinite(g).all()
+    np.testing.assert_array_equal(g, w)
+
+
 def test_training_reduces_the_loss(fluid):
     _, T = _mods()
     X, Y, info = T.generate(256, size=128, steps_per_run=64, seed=7)

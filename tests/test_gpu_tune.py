@@ -11,7 +11,7 @@ def test_autotune_picks_caches_and_keeps_parity(fluid, wl, tmp_path):
     cache = tmp_path / "tune.txt"
     kw = dict(diffuse_iterations=20, pressure_iterations=20, device=0)
     t1 = fluid.autotune(w.rows, w.cols, w.diffusion, w.viscosity, w.dt, steps=2, cache_path=cache, **kw)
-    assert t1["tile_rows"] in (64, 128) and 4 <= t1["sweeps_per_pass"] <= 16 and t1["ms_per_step"] > 0
+    assert t1["tile_rows"] in (64, 128) and 2 <= t1["sweeps_per_pass"] <= 16 and t1["ms_per_step"] > 0
     lines = cache.read_text().strip().splitlines()
     assert len(lines) == 1 and lines[0].split()[1:3] == [str(t1["tile_rows"]), str(t1["sweeps_per_pass"])]
     t2 = fluid.autotune(w.rows, w.cols, w.diffusion, w.viscosity, w.dt, steps=2, cache_path=cache, **kw)
