@@ -127,6 +127,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 for (int q = 0; q < 3; ++q) {
                     StencilField f{};
                     field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows, dplan[pass]);
+                    realign_columns(f);
                     field_diffusion(f, b->rows[g], b->cols[g], rates[q], dt);
                     f.s_lr = bnd_sign_lr(modes[q]);
                     f.s_tb = bnd_sign_tb(modes[q]);
@@ -163,6 +164,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                     StencilField f{};
                     field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows,
                                    pplan[pass] + (last ? 1 : 0));
+                    if (pass > 0) realign_columns(f);  // the divergence pass is always staged
                     const float h = grid_spacing(b->rows[g], b->cols[g]);
                     f.s_lr = f.s_tb = 1.f;
                     f.sweeps = pplan[pass];

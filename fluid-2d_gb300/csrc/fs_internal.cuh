@@ -58,6 +58,7 @@ struct StencilField {
     int halo;             // H: region = tile grown by H on each side
     int rows, cols, pitch;
     int tile_w, tile_h, tiles_x, tiles_y, shift_x, shift_y;
+    int realign;          // 1: start each region on a multiple of four columns (see realign_columns)
     int tile_begin;       // first block index of this field in the launch
     int* nonfinite;       // optional flag (epilogue outputs)
 };
@@ -132,6 +133,23 @@ inline void tile_split(int n, int tile, int* count, int* shift) {
     *count = (n + s + tile - 1) / tile;
 }
 
+// Column tiling for passes whose interior tiles can take the stencil's direct path,
+// which loads and stores a region's rows 16 bytes at a time and so needs each region to
+// start on a multiple of four columns. With tile width 128 - 2H and halo H that holds
+// for every tile when the width is a multiple of four and H + shift is too. Otherwise
+// the width shrinks by three and the kernel moves each region's start down to the
+// multiple of four below it (by a = 0..3 columns): the left margin becomes H + a and the
+// right one H + 3 - a, both at least H.
+inline void realign_columns(StencilField& f) {
+    f.realign = 0;
+    const int w = kRegionW - 2 * f.halo;
+    if (w % 4 == 0 && (f.halo + f.shift_x) % 4 == 0) return;
+    if (w - 3 < 1) return;
+    f.tile_w = w - 3;
+    tile_split(f.cols, f.tile_w, &f.tiles_x, &f.shift_x);
+    f.realign = 1;
+}
+
 // Sets the calling thread's fs_last_error() message and returns code (solver.cu).
 int record_error(int code, const char* msg);
 
@@ -171,6 +189,10 @@ cudaError_t launch_coarse_residual(const float* div, const float* p, int rows, i
                                    double* norm2, float* scale, void* xin, const int* skip_if, cudaStream_t st);
 cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* bs, const float* scale, float kappa,
                                  int G, int nu, const int* skip_if, cudaStream_t st);
+// Both candidates' smoothing in one launch (one CTA each, run side by side).
+cudaError_t launch_coarse_smooth_pair(const float* y_in_a, float* y_out_a, const float* y_in_b, float* y_out_b,
+                                      const float* bs, const float* scale, float kappa, int G, int nu,
+                                      const int* skip_if, cudaStream_t st);
 // The network input (channel 0 = bs / RMS(bs), scale, norm) from given block sums.
 cudaError_t launch_coarse_input(const float* bs, int G, float* scale, void* xin, double* norm2, const int* skip_if,
                                 cudaStream_t st);

@@ -257,38 +257,67 @@ __global__ void coarse_input_kernel(const float* __restrict__ bs, int G, float* 
 // cell-to-cell error that the fine sweeps would otherwise damp slowly; applied to zero it
 // is the classical coarse correction the network has to beat.
 constexpr int kCoarseMax = 64;
-__global__ void coarse_smooth_kernel(const float* y_in, float* y_out, const float* __restrict__ bs,
-                                     const float* __restrict__ scale_ptr, float kappa, int G, int nu,
-                                     const int* __restrict__ skip_if) {
+constexpr int kSmoothThreads = 1024;
+constexpr int kSmoothCells = kCoarseMax * kCoarseMax / kSmoothThreads;  // cells per thread
+// One CTA per candidate (blockIdx.x selects a or b): nu weighted-Jacobi sweeps of the
+// coarse equation in shared memory. Each thread keeps its cells' right-hand sides and
+// neighbour offsets in registers (the edges reflect: a missing neighbour is the cell
+// itself), so a sweep is five shared loads, the update and one store per cell.
+__global__ void __launch_bounds__(kSmoothThreads) coarse_smooth_kernel(const float* y_in_a, float* y_out_a,
+                                                                       const float* y_in_b, float* y_out_b,
+                                                                       const float* __restrict__ bs,
+                                                                       const float* __restrict__ scale_ptr,
+                                                                       float kappa, int G, int nu,
+                                                                       const int* __restrict__ skip_if) {
     if (skip_if && __ldcg(skip_if)) return;
+    const float* y_in = blockIdx.x ? y_in_b : y_in_a;
+    float* y_out = blockIdx.x ? y_out_b : y_out_a;
+    if (!y_out) return;
     __shared__ float e[2][kCoarseMax * kCoarseMax];
-    __shared__ double red[1024];
+    __shared__ double red[kSmoothThreads];
+    const int tid = threadIdx.x, n = G * G;
     const float unit = (*scale_ptr) * kappa;
-    for (int c = threadIdx.x; c < G * G; c += blockDim.x) e[0][c] = y_in ? y_in[(size_t)c * kC] * unit : 0.f;
+    for (int c = tid; c < n; c += kSmoothThreads) e[0][c] = y_in ? y_in[(size_t)c * kC] * unit : 0.f;
+    float b[kSmoothCells];
+    int up[kSmoothCells], dn[kSmoothCells], lf[kSmoothCells], rt[kSmoothCells];
+#pragma unroll
+    for (int k = 0; k < kSmoothCells; ++k) {
+        const int c = tid + k * kSmoothThreads;
+        const int I = c / G, J = c - (c / G) * G;
+        const bool in = c < n;
+        b[k] = in ? bs[c] : 0.f;
+        up[k] = in && I > 0 ? c - G : c;
+        dn[k] = in && I < G - 1 ? c + G : c;
+        lf[k] = in && J > 0 ? c - 1 : c;
+        rt[k] = in && J < G - 1 ? c + 1 : c;
+    }
     __syncthreads();
     const float w = 0.8f;
     int cur = 0;
     for (int it = 0; it < nu; ++it) {
-        for (int c = threadIdx.x; c < G * G; c += blockDim.x) {
-            const int I = c / G, J = c % G;
-            const float x = e[cur][c];
-            const float up = I > 0 ? e[cur][c - G] : x, dn = I < G - 1 ? e[cur][c + G] : x;
-            const float lf = J > 0 ? e[cur][c - 1] : x, rt = J < G - 1 ? e[cur][c + 1] : x;
-            e[cur ^ 1][c] = (1.f - w) * x + w * 0.25f * (bs[c] + up + dn + lf + rt);
+        const float* src = e[cur];
+        float* dst = e[cur ^ 1];
+#pragma unroll
+        for (int k = 0; k < kSmoothCells; ++k) {
+            const int c = tid + k * kSmoothThreads;
+            if (c < n) {
+                const float x = src[c];
+                dst[c] = (1.f - w) * x + w * 0.25f * (b[k] + src[up[k]] + src[dn[k]] + src[lf[k]] + src[rt[k]]);
+            }
         }
         __syncthreads();
         cur ^= 1;
     }
     double acc = 0.0;
-    for (int c = threadIdx.x; c < G * G; c += blockDim.x) acc += e[cur][c];
-    red[threadIdx.x] = acc;
+    for (int c = tid; c < n; c += kSmoothThreads) acc += e[cur][c];
+    red[tid] = acc;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    for (int s = kSmoothThreads / 2; s > 0; s >>= 1) {
+        if (tid < s) red[tid] += red[tid + s];
         __syncthreads();
     }
-    const float mean = (float)(red[0] / (double)(G * G));
-    for (int c = threadIdx.x; c < G * G; c += blockDim.x) y_out[(size_t)c * kC] = (e[cur][c] - mean) / unit;
+    const float mean = (float)(red[0] / (double)n);
+    for (int c = tid; c < n; c += kSmoothThreads) y_out[(size_t)c * kC] = (e[cur][c] - mean) / unit;
 }
 
 // Fine warm start: p_out = p_prev + bilinear interpolation of the coarse correction
@@ -333,23 +362,24 @@ __global__ void energy_gain_kernel(const float* __restrict__ div, const float* _
                                    double* __restrict__ out, const int* __restrict__ skip_if) {
     if (skip_if && __ldcg(skip_if)) return;
     __shared__ double red[256];
-    double g = 0.0;
-    const long n = (long)(rows - 2) * (cols - 2);
-    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(e / (cols - 2)), j = 1 + (int)(e % (cols - 2));
-        const size_t o = (size_t)i * pitch + j;
-        const float pc = p_cur[o];
-        const float r = div[o] + (p_cur[o - 1] + p_cur[o + 1]) + (p_cur[o - pitch] + p_cur[o + pitch]) - 4.f * pc;
-        const float c = p_try[o] - pc;
-        const float cl = p_try[o - 1] - p_cur[o - 1], cr = p_try[o + 1] - p_cur[o + 1];
-        const float cu = p_try[o - pitch] - p_cur[o - pitch], cd = p_try[o + pitch] - p_cur[o + pitch];
-        const float ac = 4.f * c - ((cl + cr) + (cu + cd));
-        g += 2.0 * (double)c * r - (double)c * ac;
+    float g = 0.f;  // a thread's few cells; the CTA and grid sums are in FP64
+    const int j = blockIdx.x * 256 + threadIdx.x;
+    if (j >= 1 && j <= cols - 2) {
+        for (int i = 1 + blockIdx.y; i <= rows - 2; i += gridDim.y) {
+            const size_t o = (size_t)i * pitch + j;
+            const float pc = p_cur[o];
+            const float r = div[o] + (p_cur[o - 1] + p_cur[o + 1]) + (p_cur[o - pitch] + p_cur[o + pitch]) - 4.f * pc;
+            const float c = p_try[o] - pc;
+            const float cl = p_try[o - 1] - p_cur[o - 1], cr = p_try[o + 1] - p_cur[o + 1];
+            const float cu = p_try[o - pitch] - p_cur[o - pitch], cd = p_try[o + pitch] - p_cur[o + pitch];
+            const float ac = 4.f * c - ((cl + cr) + (cu + cd));
+            g += 2.f * c * r - c * ac;
+        }
     }
     red[threadIdx.x] = g;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
         __syncthreads();
     }
     if (threadIdx.x == 0) atomicAdd(out, red[0]);
@@ -448,33 +478,65 @@ __global__ void accept_best_kernel(float* __restrict__ p_cur, const float* __res
 //
 // r = div + sum(nbrs (p_hi + p_lo)) - 4 (p_hi + p_lo) on the interior in FP64, stored in
 // FP32 (edges 0); sums[0] += ||r||^2, sums[1] += ||div||^2 (FP64, zeroed before).
+// Double-float arithmetic on the FP32 pipe (GB300's FP64 rate is a small fraction of its
+// FP32 rate): two_sum is the error-free transformation a + b = s + e (Knuth, TAOCP vol. 2,
+// 4.2.2; Moller 1965); sum2 accumulates terms with their rounding errors (Ogita, Rump,
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005), so a sum comes
+// out as if computed in twice the working precision.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Rows per CTA row-slab of the row-wise kernels below (blockIdx.x: 256-column slice).
+inline dim3 row_grid(int rows, int cols) {
+    const int gx = (cols + 255) / 256;
+    const int gy = std::max(1, std::min(rows, 2048 / gx));
+    return dim3(gx, gy);
+}
+
+// r = div + sum(nbrs of p) - 4p for p = p_hi + p_lo, to about twice FP32 precision: the
+// FP32 heads (and div, and -4*p_hi, which is exact) are summed with their rounding errors
+// (sum2), the tails, which are ~2^-24 of the heads, in FP32; zero on the boundary.
+// sums[0] += ||r||^2 and sums[1] += ||div||^2 over the interior.
 __global__ void residual_df_kernel(const float* __restrict__ div, const float* __restrict__ ph,
                                    const float* __restrict__ pl, float* __restrict__ r, int rows, int cols, int pitch,
                                    double* __restrict__ sums) {
     __shared__ double red[2][256];
-    double rr = 0.0, dd = 0.0;
-    const long n = (long)rows * cols;
-    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(e / cols), j = (int)(e % cols);
-        const size_t o = (size_t)i * pitch + j;
-        if (i < 1 || i > rows - 2 || j < 1 || j > cols - 2) {
-            r[o] = 0.f;
-            continue;
+    float rr = 0.f, dd = 0.f;
+    const int j = blockIdx.x * 256 + threadIdx.x;
+    if (j < cols) {
+        for (int i = blockIdx.y; i < rows; i += gridDim.y) {
+            const size_t o = (size_t)i * pitch + j;
+            if (i < 1 || i > rows - 2 || j < 1 || j > cols - 2) {
+                r[o] = 0.f;
+                continue;
+            }
+            const float dv = div[o];
+            const float t[5] = {ph[o - 1], ph[o + 1], ph[o - pitch], ph[o + pitch], __fmul_rn(-4.f, ph[o])};
+            float sh = dv, sl = 0.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                float e;
+                two_sum(sh, t[k], sh, e);
+                sl = __fadd_rn(sl, e);
+            }
+            const float lo = __fsub_rn(__fadd_rn(__fadd_rn(pl[o - 1], pl[o + 1]), __fadd_rn(pl[o - pitch], pl[o + pitch])),
+                                       __fmul_rn(4.f, pl[o]));
+            const float res = __fadd_rn(sh, __fadd_rn(sl, lo));
+            r[o] = res;
+            rr = fmaf(res, res, rr);
+            dd = fmaf(dv, dv, dd);
         }
-        auto P = [&](size_t q) { return (double)ph[q] + (double)pl[q]; };
-        const double dv = (double)div[o];
-        const double res = dv + ((P(o - 1) + P(o + 1)) + (P(o - pitch) + P(o + pitch))) - 4.0 * P(o);
-        r[o] = (float)res;
-        rr += res * res;
-        dd += dv * dv;
     }
     red[0][threadIdx.x] = rr;
     red[1][threadIdx.x] = dd;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            red[0][threadIdx.x] += red[0][threadIdx.x + s];
-            red[1][threadIdx.x] += red[1][threadIdx.x + s];
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + k];
+            red[1][threadIdx.x] += red[1][threadIdx.x + k];
         }
         __syncthreads();
     }
@@ -483,16 +545,17 @@ __global__ void residual_df_kernel(const float* __restrict__ div, const float* _
         atomicAdd(sums + 1, red[1][0]);
     }
 }
-
-// (p_hi, p_lo) += e: t = p_hi + p_lo + e in FP64, p_hi = RN(t), p_lo = RN(t - p_hi), on
-// every cell (edges included, so both parts keep their Neumann fill).
+// (p_hi, p_lo) += e as a double-float sum: two_sum of the heads, the error folded into
+// the tail, renormalised (fast two_sum: the new head dominates).
 __global__ void accumulate_df_kernel(float* __restrict__ ph, float* __restrict__ pl, const float* __restrict__ e,
                                      long n) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-        const double t = ((double)ph[k] + (double)pl[k]) + (double)e[k];
-        const float hi = (float)t;
+        float s, err;
+        two_sum(ph[k], e[k], s, err);
+        const float lo = __fadd_rn(pl[k], err);
+        const float hi = __fadd_rn(s, lo);
         ph[k] = hi;
-        pl[k] = (float)(t - (double)hi);
+        pl[k] = __fsub_rn(lo, __fsub_rn(hi, s));
     }
 }
 
@@ -526,7 +589,17 @@ cudaError_t launch_coarse_interp(const float* y, float* e, int G, const float* s
 cudaError_t launch_coarse_smooth(const float* y_in, float* y_out, const float* bs, const float* scale, float kappa,
                                  int G, int nu, const int* skip_if, cudaStream_t st) {
     if (G > kCoarseMax) return cudaErrorInvalidValue;
-    coarse_smooth_kernel<<<1, 1024, 0, st>>>(y_in, y_out, bs, scale, kappa, G, nu, skip_if);
+    coarse_smooth_kernel<<<1, kSmoothThreads, 0, st>>>(y_in, y_out, nullptr, nullptr, bs, scale, kappa, G, nu,
+                                                       skip_if);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coarse_smooth_pair(const float* y_in_a, float* y_out_a, const float* y_in_b, float* y_out_b,
+                                      const float* bs, const float* scale, float kappa, int G, int nu,
+                                      const int* skip_if, cudaStream_t st) {
+    if (G > kCoarseMax) return cudaErrorInvalidValue;
+    coarse_smooth_kernel<<<2, kSmoothThreads, 0, st>>>(y_in_a, y_out_a, y_in_b, y_out_b, bs, scale, kappa, G, nu,
+                                                       skip_if);
     return cudaGetLastError();
 }
 
@@ -547,7 +620,7 @@ cudaError_t launch_damp(const float* div, const float* p, float* out, int rows, 
 
 cudaError_t launch_energy_gain(const float* div, const float* p_cur, const float* p_try, int rows, int cols,
                                int pitch, double* out, const int* skip_if, cudaStream_t st) {
-    energy_gain_kernel<<<152 * 4, 256, 0, st>>>(div, p_cur, p_try, rows, cols, pitch, out, skip_if);
+    energy_gain_kernel<<<row_grid(rows, cols), 256, 0, st>>>(div, p_cur, p_try, rows, cols, pitch, out, skip_if);
     return cudaGetLastError();
 }
 
@@ -559,9 +632,7 @@ cudaError_t launch_accept_best(float* p_cur, const float* pa, const float* pb, l
 
 cudaError_t launch_residual_df(const float* div, const float* p_hi, const float* p_lo, float* r, int rows, int cols,
                                int pitch, double* sums, cudaStream_t st) {
-    const long n = (long)rows * cols;
-    const int blocks = (int)std::min<long>((n + 255) / 256, 4096);
-    residual_df_kernel<<<blocks, 256, 0, st>>>(div, p_hi, p_lo, r, rows, cols, pitch, sums);
+    residual_df_kernel<<<row_grid(rows, cols), 256, 0, st>>>(div, p_hi, p_lo, r, rows, cols, pitch, sums);
     return cudaGetLastError();
 }
 

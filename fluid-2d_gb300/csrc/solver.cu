@@ -334,6 +334,7 @@ int enqueue_diffuse(fs_solver* s, const int* fields, int nf, const float* rates,
             const int fid = fields[q];
             StencilField& f = L.f[q];
             set_geometry(f, s, plan[pass]);
+            realign_columns(f);
             diffuse_constants(f, s->rows, s->cols, rates[q], dt);
             const int mode = fid == F_D ? BND_CONT : (fid == F_U ? BND_OPP_H : BND_OPP_V);
             f.s_lr = bnd_sign_lr(mode);
@@ -470,35 +471,32 @@ int enqueue_network_correction(fs_solver* s, const float* rhs, float* p_cur, con
     }
     // candidate A: the network's correction, post-smoothed; B: the coarse smoothing alone
     float* pb = s->p[1];  // free between pressure passes
-    CK(launch_coarse_smooth(s->net.y, s->net.y, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
-                            s->stream));
-    CK(launch_coarse_smooth(nullptr, s->net.yc, s->net.bs, s->net.scale, kappa, G, kCoarseSweeps, converged,
-                            s->stream));
+    CK(launch_coarse_smooth_pair(s->net.y, s->net.y, nullptr, s->net.yc, s->net.bs, s->net.scale, kappa, G,
+                                 kCoarseSweeps, converged, s->stream));
     if (G2) {
         // both candidates continue on the finer coarse level, then go to the fine grid
         CK(launch_coarse_interp(s->net.y, s->net.e2a, G, s->net.scale, kappa, converged, s->stream));
         CK(launch_coarse_interp(s->net.yc, s->net.e2b, G, s->net.scale, kappa, converged, s->stream));
-        CK(launch_coarse_smooth(s->net.e2a, s->net.e2a, s->net.bs2, s->net.one, 1.f, G2, kCoarseSweepsFine, converged,
-                                s->stream));
-        CK(launch_coarse_smooth(s->net.e2b, s->net.e2b, s->net.bs2, s->net.one, 1.f, G2, kCoarseSweepsFine, converged,
-                                s->stream));
+        CK(launch_coarse_smooth_pair(s->net.e2a, s->net.e2a, s->net.e2b, s->net.e2b, s->net.bs2, s->net.one, 1.f, G2,
+                                     kCoarseSweepsFine, converged, s->stream));
         CK(launch_prolong(s->net.e2a, p_cur, s->pguess, s->rows, s->cols, s->pitch, G2, s->net.one, 1.f, converged,
                           s->stream));
         CK(launch_prolong(s->net.e2b, p_cur, pb, s->rows, s->cols, s->pitch, G2, s->net.one, 1.f, converged,
                           s->stream));
-        cnt.launches += 4;
+        cnt.launches += 5;
     } else {
         CK(launch_prolong(s->net.y, p_cur, s->pguess, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
                           s->stream));
         CK(launch_prolong(s->net.yc, p_cur, pb, s->rows, s->cols, s->pitch, G, s->net.scale, kappa, converged,
                           s->stream));
+        cnt.launches += 2;
     }
     CK(cudaMemsetAsync(s->net.res + 1, 0, 2 * sizeof(double), s->stream));
     CK(launch_energy_gain(rhs, p_cur, s->pguess, s->rows, s->cols, s->pitch, s->net.res + 1, converged, s->stream));
     CK(launch_energy_gain(rhs, p_cur, pb, s->rows, s->cols, s->pitch, s->net.res + 2, converged, s->stream));
     CK(launch_accept_best(p_cur, s->pguess, pb, (long)s->field_floats, s->net.res + 1, converged, s->net.counters,
                           s->stream));
-    cnt.launches += 9;
+    cnt.launches += 4;  // the smoothing pair, two energy gains, the choice
     return FS_OK;
 }
 
@@ -596,6 +594,7 @@ int enqueue_project_learned_cycles(fs_solver* s, const float* u_in, const float*
     CK(cudaMemsetAsync(s->ctrl + slot, 0, sizeof(SolveCtrl), s->stream));
     PressureSolve P{};
     set_geometry(P.mid, s, K + 1);
+    realign_columns(P.mid);  // interior tiles take the direct path (P.first copies the tiling)
     P.mid.s_lr = P.mid.s_tb = 1.f;
     P.mid.sweeps = K;
     P.mid.h = grid_h(s->rows, s->cols);
@@ -659,6 +658,7 @@ int enqueue_project_learned_defect(fs_solver* s, const float* u_in, const float*
     double* hsums = reinterpret_cast<double*>(s->host_ctrl + 1);
     PressureSolve P{};
     set_geometry(P.mid, s, K + 1);
+    realign_columns(P.mid);  // interior tiles take the direct path (P.first copies the tiling)
     P.mid.s_lr = P.mid.s_tb = 1.f;
     P.mid.sweeps = K;
     P.mid.h = grid_h(s->rows, s->cols);
@@ -738,6 +738,7 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
     PressureSolve P{};
     for (StencilField* f : {&P.first, &P.mid}) {
         set_geometry(*f, s, K + 1);
+        realign_columns(*f);  // one tiling for both; the middle passes' interior tiles go direct
         f->s_lr = f->s_tb = 1.f;
         f->sweeps = K;
         f->cdiv = -0.5f * h;
@@ -787,16 +788,8 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
 int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u_out, float* v_out, int slot,
                     Counter& cnt) {
     if (s->cfg.pressure_tolerance > 0.f) return enqueue_project_to_residual(s, u_in, v_in, u_out, v_out, slot, cnt);
-    std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
+    const std::vector<int> plan = split_sweeps(s->cfg.pressure_iterations, s->sweeps);
     const int m = (int)plan.size();
-    // The last pass needs one ring more than its sweeps for the gradient. When that would
-    // make its halo one more than a multiple of four, it gives one sweep to the first
-    // pass: its halo then matches the middle passes' and its interior tiles take the
-    // direct path (16-byte aligned regions). The sweeps run in the same order either way.
-    if (m >= 2 && plan[m - 1] >= 1 && plan[m - 1] % 4 == 0 && plan[0] + 1 <= stencil_max_halo(s->tile_rows) - 1) {
-        plan[0] += 1;
-        plan[m - 1] -= 1;
-    }
     const bool warm = s->cfg.warm_start != FS_WARM_ZERO;
     const float h = grid_h(s->rows, s->cols);
     const float* pin = nullptr;
@@ -808,6 +801,7 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
         L.nfields = 1;
         StencilField& f = L.f[0];
         set_geometry(f, s, plan[pass] + (last ? 1 : 0));
+        if (pass > 0) realign_columns(f);  // the first pass (divergence) is always staged
         f.s_lr = f.s_tb = 1.f;
         f.sweeps = plan[pass];
         f.cdiv = -0.5f * h;

@@ -330,16 +330,20 @@ __device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi,
 // final field straight back from registers, without staging the region in shared
 // memory ("direct" tiles). Requires the region's first column and the row pitch to be
 // multiples of four floats and the buffers 16-byte aligned (checked by the caller).
+// Flags of a tile's sweep phase.
+constexpr int kSwEdge = 1;    // a domain-edge tile (edge folding in the sweeps)
+constexpr int kSwDirect = 2;  // a direct tile (global <-> registers)
+constexpr int kSwFirst = 4;   // direct: first diffusion pass (add_sources fused)
+constexpr int kSwResid = 8;   // direct: residual partial sums wanted
 struct SweepParams {
-    int nsweeps, edge, gy0, gx0, rows, cols;
+    int nsweeps, flags, gy0, gx0, rows, cols;
     float s_lr, s_tb, a, dh, dl, rf;
     // direct tiles only
-    int direct;
     const float* x;  // field in
     const float* k;  // constant term in (x0 / div), or the source s of a first diffusion pass
     float* y;        // field out (output tile; may be null)
     float* kout;     // first diffusion pass: x0 out (output tile; may be null)
-    int pitch, halo, tile_h, tile_w, first;
+    int pitch, halo, halo_l, tile_h, tile_w;  // halo_l: left margin (columns)
     float dt;
     const StencilField* F;  // last pressure pass: the gradient epilogue's fields (else null)
 };
@@ -371,6 +375,17 @@ __device__ __forceinline__ void gradient_direct(const float2 (&X)[4][4], int eof
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ float4 smem4[];
     float* const E = reinterpret_cast<float*>(smem4) + eoff;
+    const bool out_cols = c_lo < 4 && c_hi > 0;
+    auto pv = [&](int ii, int q) -> float { return (ii >> 2) ? X[ii & 3][q].y : X[ii & 3][q].x; };
+    auto live = [&](int i) { return out_cols && i >= r_lo && i < r_hi; };
+    // u and v of the first four rows are loaded before the exchange's barrier, so their
+    // latency overlaps it; those of the last four rows are loaded together
+    float4 uu[4], vv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        uu[i] = live(i) ? __ldcg(reinterpret_cast<const float4*>(F.u_in + o + i * pitch)) : make_float4(0, 0, 0, 0);
+        vv[i] = live(i) ? __ldcg(reinterpret_cast<const float4*>(F.v_in + o + i * pitch)) : make_float4(0, 0, 0, 0);
+    }
     const int my_top = (2 * w) * RW + 4 * lane, my_bot = my_top + RW;
     const int nb_up = w > 0 ? my_top - RW : my_top;
     const int nb_dn = w < NW - 1 ? my_top + 2 * RW : my_bot;
@@ -381,34 +396,107 @@ __device__ __forceinline__ void gradient_direct(const float2 (&X)[4][4], int eof
     const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn);
     const float up[4] = {u4.x, u4.y, u4.z, u4.w}, dn[4] = {d4.x, d4.y, d4.z, d4.w};
     const float h = F.h, rh = __frcp_rn(h);
-    const bool out_cols = c_lo < 4 && c_hi > 0;
     int bad = 0;
 #pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        float L0[4], R3[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = half * 4 + k;
+            L0[k] = __shfl_up_sync(FULL, pv(i, 3), 1);
+            R3[k] = __shfl_down_sync(FULL, pv(i, 0), 1);
+        }
+        float4 un4[4], vn4[4];
+        if (half == 1) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int i = 4 + k;
+                uu[k] = live(i) ? __ldcg(reinterpret_cast<const float4*>(F.u_in + o + i * pitch)) : make_float4(0, 0, 0, 0);
+                vv[k] = live(i) ? __ldcg(reinterpret_cast<const float4*>(F.v_in + o + i * pitch)) : make_float4(0, 0, 0, 0);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = half * 4 + k;
+            const float uin[4] = {uu[k].x, uu[k].y, uu[k].z, uu[k].w}, vin[4] = {vv[k].x, vv[k].y, vv[k].z, vv[k].w};
+            float un[4], vn[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float pl = q > 0 ? pv(i, q - 1) : L0[k];
+                const float pr = q < 3 ? pv(i, q + 1) : R3[k];
+                const float pu = i > 0 ? pv(i - 1, q) : up[q];
+                const float pd = i < 7 ? pv(i + 1, q) : dn[q];
+                const float gu = div_by(__fmul_rn(0.5f, __fsub_rn(pr, pl)), h, rh);
+                const float gv = div_by(__fmul_rn(0.5f, __fsub_rn(pd, pu)), h, rh);
+                un[q] = __fsub_rn(uin[q], gu);
+                vn[q] = __fsub_rn(vin[q], gv);
+                if (live(i) && q >= c_lo && q < c_hi) bad |= !(isfinite(un[q]) && isfinite(vn[q]));
+            }
+            un4[k] = make_float4(un[0], un[1], un[2], un[3]);
+            vn4[k] = make_float4(vn[0], vn[1], vn[2], vn[3]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = half * 4 + k;
+            if (!live(i)) continue;
+            store_row4(F.u_out + o + i * pitch, un4[k], c_lo, c_hi);
+            store_row4(F.v_out + o + i * pitch, vn4[k], c_lo, c_hi);
+        }
+    }
+    if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
+}
+
+// Residual partial sums of a direct tile of a residual-target pass: over the output cells,
+// ||div + R + L + D + U - 4p||^2 and ||div||^2 of the final pressure block in registers,
+// div read back from this thread's constant terms (K, kidx layout), the neighbours by
+// shuffles and one more row exchange (in the buffer the last sweep did not use). Interior
+// tiles only, so every output cell is an interior cell. Returns (rnum, rden).
+template <int NW>
+__device__ __forceinline__ float2 residual_direct(const float2 (&X)[4][4], int eoff, const float* __restrict__ K,
+                                                  int w, int lane, int r_lo, int r_hi, int c_lo, int c_hi) {
+    constexpr int RW = kRegionW;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ float4 smem4[];
+    float* const E = reinterpret_cast<float*>(smem4) + eoff;
+    const int my_top = (2 * w) * RW + 4 * lane, my_bot = my_top + RW;
+    const int nb_up = w > 0 ? my_top - RW : my_top;
+    const int nb_dn = w < NW - 1 ? my_top + 2 * RW : my_bot;
+    *reinterpret_cast<float4*>(E + my_top) = make_float4(X[0][0].x, X[0][1].x, X[0][2].x, X[0][3].x);
+    *reinterpret_cast<float4*>(E + my_bot) = make_float4(X[3][0].y, X[3][1].y, X[3][2].y, X[3][3].y);
+    __syncthreads();
+    const float4 u4 = *reinterpret_cast<const float4*>(E + nb_up);
+    const float4 d4 = *reinterpret_cast<const float4*>(E + nb_dn);
+    const float up[4] = {u4.x, u4.y, u4.z, u4.w}, dn[4] = {d4.x, d4.y, d4.z, d4.w};
+    auto pv = [&](int ii, int q) -> float { return (ii >> 2) ? X[ii & 3][q].y : X[ii & 3][q].x; };
+    const bool out_cols = c_lo < 4 && c_hi > 0;
+    float rnum = 0.f, rden = 0.f;
+#pragma unroll
     for (int i = 0; i < 8; ++i) {
-        auto pv = [&](int ii, int q) -> float { return (ii >> 2) ? X[ii & 3][q].y : X[ii & 3][q].x; };
         const float L0 = __shfl_up_sync(FULL, pv(i, 3), 1);
         const float R3 = __shfl_down_sync(FULL, pv(i, 0), 1);
-        if (i < r_lo || i >= r_hi || !out_cols) continue;
-        const float4 ui = __ldcg(reinterpret_cast<const float4*>(F.u_in + o + i * pitch));
-        const float4 vi = __ldcg(reinterpret_cast<const float4*>(F.v_in + o + i * pitch));
-        const float uin[4] = {ui.x, ui.y, ui.z, ui.w}, vin[4] = {vi.x, vi.y, vi.z, vi.w};
-        float un[4], vn[4];
+        if (!out_cols || i < r_lo || i >= r_hi) continue;
+        const int j = i & 3, hsel = i >> 2;
+        const float4 ka = *reinterpret_cast<const float4*>(K + j * (2 * RW));
+        const float4 kb = *reinterpret_cast<const float4*>(K + j * (2 * RW) + RW);
+        const float kk[4] = {hsel ? ka.y : ka.x, hsel ? ka.w : ka.z, hsel ? kb.y : kb.x, hsel ? kb.w : kb.z};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
+            if (q < c_lo || q >= c_hi) continue;
             const float pl = q > 0 ? pv(i, q - 1) : L0;
             const float pr = q < 3 ? pv(i, q + 1) : R3;
             const float pu = i > 0 ? pv(i - 1, q) : up[q];
             const float pd = i < 7 ? pv(i + 1, q) : dn[q];
-            const float gu = div_by(__fmul_rn(0.5f, __fsub_rn(pr, pl)), h, rh);
-            const float gv = div_by(__fmul_rn(0.5f, __fsub_rn(pd, pu)), h, rh);
-            un[q] = __fsub_rn(uin[q], gu);
-            vn[q] = __fsub_rn(vin[q], gv);
-            if (q >= c_lo && q < c_hi) bad |= !(isfinite(un[q]) && isfinite(vn[q]));
+            // the staged residual's order: div + R + L + D + U - 4p
+            float sres = __fadd_rn(kk[q], pr);
+            sres = __fadd_rn(sres, pl);
+            sres = __fadd_rn(sres, pd);
+            sres = __fadd_rn(sres, pu);
+            const float res = __fsub_rn(sres, __fmul_rn(4.f, pv(i, q)));
+            rnum = fmaf(res, res, rnum);
+            rden = fmaf(kk[q], kk[q], rden);
         }
-        store_row4(F.u_out + o + i * pitch, make_float4(un[0], un[1], un[2], un[3]), c_lo, c_hi);
-        store_row4(F.v_out + o + i * pitch, make_float4(vn[0], vn[1], vn[2], vn[3]), c_lo, c_hi);
     }
-    if (bad && F.nonfinite) atomicOr(F.nonfinite, 1);
+    return make_float2(rnum, rden);
 }
 
 // The sweeps of one tile in the block layout of run_sweeps. Staged tiles: the field
@@ -418,7 +506,15 @@ __device__ __forceinline__ void gradient_direct(const float2 (&X)[4][4], int eof
 // field's buffer. Kept out of line so that the tile body's other live values are saved
 // once around the call instead of competing with the register blocks, and so that
 // staged and direct interior tiles share one copy of the sweep loop.
-// MODE: 0 staged tiles only, 1 also direct tiles, 2 also the direct gradient epilogue.
+// MODE bits: 1 direct tiles, 2 the direct gradient epilogue, 4 the direct residual sums.
+// A direct residual tile leaves its thread's partial sums (rnum, rden) in shared memory
+// at resid_slot(), in the exchange buffer the last sweep used (free once every warp has
+// passed the final exchange's barrier).
+constexpr int kModeDirect = 1, kModeGrad = 2, kModeResid = 4;
+template <int NW>
+__device__ __forceinline__ int resid_slot(int xoff, int nsweeps, int tid) {
+    return xoff + (((nsweeps & 1) ^ 1) * (2 * NW * kRegionW)) + 2 * tid;
+}
 template <bool DIFF, int NW, int MODE>
 __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P) {
     constexpr int RW = kRegionW;
@@ -433,17 +529,17 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
     // direct tiles: output rows [r_lo, r_hi) and columns [c_lo, c_hi) relative to this
     // thread's block
     const int r_lo = P.halo - rb, r_hi = P.halo + P.tile_h - rb;
-    const int c_lo = P.halo - cb, c_hi = P.halo + P.tile_w - cb;
+    const int c_lo = P.halo_l - cb, c_hi = P.halo_l + P.tile_w - cb;
     const bool out_cols = c_lo < 4 && c_hi > 0;
     float2 xb[4][4];
-    if (MODE > 0 && P.direct) {
+    if ((MODE & kModeDirect) && (P.flags & kSwDirect)) {
         float* const K = S + koff + w * (8 * RW) + 4 * lane;
         float4 t[8], kk[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) t[i] = __ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch));
 #pragma unroll
         for (int i = 0; i < 8; ++i) kk[i] = __ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch));
-        if (P.first) {
+        if (P.flags & kSwFirst) {
             // add_sources_kernel (fluid_solver_gpu.cu:64), fused as compiled: x0 = x + dt*s
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
@@ -485,7 +581,7 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
     }
     const Coef2 c = {make_float2(P.a, P.a), make_float2(-P.dh, -P.dh), make_float2(-P.dl, -P.dl),
                      make_float2(P.rf, P.rf)};
-    if (P.edge) {
+    if (P.flags & kSwEdge) {
         const int gyb = P.gy0 + rb, gxb = P.gx0 + cb;
         const EdgeGeom g = {1 - gyb, P.rows - 2 - gyb, 1 - gxb, P.cols - 2 - gxb, P.s_lr, P.s_tb};
         run_sweeps<DIFF, true, NW>(xb, koff, xoff, P.nsweeps, w, lane, g, c);
@@ -493,7 +589,7 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
         const EdgeGeom g = {-1, -1, -1, -1, P.s_lr, P.s_tb};
         run_sweeps<DIFF, false, NW>(xb, koff, xoff, P.nsweeps, w, lane, g, c);
     }
-    if (MODE > 0 && P.direct) {
+    if ((MODE & kModeDirect) && (P.flags & kSwDirect)) {
         if (P.y != nullptr && out_cols) {
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
@@ -504,8 +600,14 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
                 store_row4(P.y + o + i * pitch, v, c_lo, c_hi);
             }
         }
-        if (MODE > 1 && P.F != nullptr) gradient_direct<NW>(xb, xoff + (P.nsweeps & 1) * (2 * NW * RW), w, lane, o, pitch, r_lo,
-                                                r_hi, c_lo, c_hi, *P.F);
+        const int efin = xoff + (P.nsweeps & 1) * (2 * NW * RW);  // exchange buffer the last sweep did not use
+        if ((MODE & kModeGrad) && P.F != nullptr)
+            gradient_direct<NW>(xb, efin, w, lane, o, pitch, r_lo, r_hi, c_lo, c_hi, *P.F);
+        if ((MODE & kModeResid) && (P.flags & kSwResid)) {
+            const float2 r =
+                residual_direct<NW>(xb, efin, S + koff + w * (8 * RW) + 4 * lane, w, lane, r_lo, r_hi, c_lo, c_hi);
+            *reinterpret_cast<float2*>(S + resid_slot<NW>(xoff, P.nsweeps, tid)) = r;
+        }
         return;  // the next tile's first barrier orders the exchange area's reuse
     }
     __syncthreads();  // every warp has read its last exchange rows
@@ -526,7 +628,7 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
 // partial sums (for residual-driven pressure solves). xin/yout stand in for F.x/F.y so
 // a persistent caller can ping-pong buffers across passes.
 // MODE as for sweep_phase.
-template <int TY, int SRB, bool DIFF, int MODE = 2>
+template <int TY, int SRB, bool DIFF, int MODE = kModeDirect | kModeGrad>
 __device__ __forceinline__ void process_tile(const StencilField& F, int b, const float* __restrict__ xin,
                                              float* __restrict__ yout, bool resid,
                                              float& rnum, float& rden) {
@@ -544,7 +646,11 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     tile_coords(b, F.tiles_x, F.tiles_y, tyi, txi);
     const int H = F.halo;
     const int gy0 = tyi * F.tile_h - F.shift_y - H;
-    const int gx0 = txi * F.tile_w - F.shift_x - H;
+    // region start column; a realigned tiling moves it down to a multiple of four, which
+    // widens the left margin to HL (the tile width leaves room on the right)
+    const int gx0h = txi * F.tile_w - F.shift_x - H;
+    const int gx0 = F.realign ? (gx0h & ~3) : gx0h;
+    const int HL = H + (gx0h - gx0);
     const int rows = F.rows, cols = F.cols;
     const size_t pitch = (size_t)F.pitch;
     const int kind = F.kind;
@@ -556,7 +662,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
 
-    if (MODE > 0 && !edge_cta && !resid && kind != PASS_PRESSURE_FIRST && F.sweeps > 0 && (MODE > 1 || !F.epilogue) &&
+    if ((MODE & kModeDirect) && !edge_cta && (!resid || (MODE & kModeResid)) && kind != PASS_PRESSURE_FIRST &&
+        F.sweeps > 0 && ((MODE & kModeGrad) || !F.epilogue) &&
         (((gx0 | F.pitch) & 3) == 0) &&
         ((reinterpret_cast<uintptr_t>(xin) | reinterpret_cast<uintptr_t>(F.x2) |
           reinterpret_cast<uintptr_t>(F.cst) | reinterpret_cast<uintptr_t>(yout) |
@@ -564,20 +671,26 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
           reinterpret_cast<uintptr_t>(F.v_in) | reinterpret_cast<uintptr_t>(F.u_out) |
           reinterpret_cast<uintptr_t>(F.v_out)) & 15) == 0) {
         const bool first = kind == PASS_DIFFUSE_FIRST;
-        SweepParams P = {F.sweeps, 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
-        P.direct = 1;
+        SweepParams P = {F.sweeps, kSwDirect | (first ? kSwFirst : 0) | (resid ? kSwResid : 0), gy0, gx0, rows, cols,
+                         F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
         P.x = xin;
         P.k = first ? F.x2 : F.cst;
         P.y = yout;
         P.kout = first ? F.cst_out : nullptr;
         P.pitch = F.pitch;
         P.halo = H;
+        P.halo_l = HL;
         P.tile_h = F.tile_h;
         P.tile_w = F.tile_w;
-        P.first = first ? 1 : 0;
         P.dt = F.dt;
         P.F = (!DIFF && F.epilogue) ? &F : nullptr;
         sweep_phase<DIFF, NW, MODE>(0, RH * RW, P);
+        if ((MODE & kModeResid) && resid) {
+            const float2 r = *reinterpret_cast<const float2*>(
+                S + resid_slot<NW>(0, F.sweeps, threadIdx.y * RW + threadIdx.x));
+            rnum += r.x;
+            rden += r.y;
+        }
         return;
     }
 
@@ -658,8 +771,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 
     // ------------------------------------------------------------------ sweeps
     if (F.sweeps > 0) {
-        SweepParams P = {F.sweeps, edge_cta ? 1 : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
-        P.direct = 0;
+        SweepParams P = {F.sweeps, edge_cta ? kSwEdge : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
         P.F = nullptr;
         sweep_phase<DIFF, NW, MODE>(co, no, P);
         if (edge_cta) {
@@ -681,7 +793,7 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     // final values of this thread's column: XREF(i) (S + co is complete after the last barrier)
 
     // ------------------------------------------------------------------ store
-    const bool col_out = col_in && tx >= H && tx < H + F.tile_w;
+    const bool col_out = col_in && tx >= HL && tx < HL + F.tile_w;
     const unsigned m_out = col_out ? (range(H - r0, H + F.tile_h - r0) & m_in) : 0u;
     if (m_out) {
         float* __restrict__ y = yout;
@@ -936,9 +1048,9 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 template <int TY, int SRB>
 __device__ __noinline__ void pressure_tile(const StencilField& F, int t, const float* x, float* y, bool resid,
                                            float& rn, float& rd) {
-    // staged tiles only: the passes of a residual solve need the staged layout for the
-    // residual sums, and the direct paths' extra live values would spill in this call chain
-    process_tile<TY, SRB, false, 0>(F, t, x, y, resid, rn, rd);
+    // direct tiles with the residual sums in registers; the final gradient pass (zero
+    // sweeps) stays staged
+    process_tile<TY, SRB, false, kModeDirect | kModeResid>(F, t, x, y, resid, rn, rd);
 }
 
 template <int TY, int SRB>
