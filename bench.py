@@ -95,7 +95,8 @@ def parse():
 # ncu on this build (profiles/stencil_kernel_2048_vortex.md): DRAM bytes read + written per
 # interior cell and field by one depth-8 pass at 2048^2, and the unit that bounds the pass
 NCU_DRAM_BYTES_PER_CELL_FIELD_PASS = 8.2
-NCU_BINDING = "SM instruction issue (ncu: issue active ~64 %, DRAM ~11 % of peak)"
+NCU_BINDING = ("instruction issue and latency: 2 CTAs of 8 warps per SM at 128 registers (24 % of the warp "
+               "slots); ncu on a 2048^2 middle pressure pass: issue active 40 %, DRAM 15 %, L1/shared 51 %")
 
 
 def dist_env():
@@ -431,6 +432,7 @@ def run_ours(a):
                              "traffic_source": "ncu dram__bytes_read+write per field-pass at 2048^2, depth 8 "
                                                f"({NCU_DRAM_BYTES_PER_CELL_FIELD_PASS} B per cell), "
                                                "profiles/stencil_kernel_2048_vortex.md",
+                             "dram_frac": ((traffic / (ms_launch / 1e3) / 1e9) / peak) if traffic else None,
                              "model_equivalent_GBps": model_gbps, "model_equivalent_frac": model_gbps / peak,
                              "model": "per-sweep model, 12 B per cell and field per sweep (the reference's "
                                       "one-kernel-per-sweep traffic)",

@@ -164,7 +164,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                     StencilField f{};
                     field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows,
                                    pplan[pass] + (last ? 1 : 0));
-                    if (pass > 0) realign_columns(f);  // the divergence pass is always staged
+                    realign_columns(f);
                     const float h = grid_spacing(b->rows[g], b->cols[g]);
                     f.s_lr = f.s_tb = 1.f;
                     f.sweeps = pplan[pass];

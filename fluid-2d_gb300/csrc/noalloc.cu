@@ -126,7 +126,7 @@ extern "C" int fs_project_noalloc(const float* u, const float* v, float* u_out, 
         f.tile_h = tile_rows - 2 * halo;
         tile_split(cols, f.tile_w, &f.tiles_x, &f.shift_x);
         tile_split(rows, f.tile_h, &f.tiles_y, &f.shift_y);
-        if (pass > 0) realign_columns(f);  // the divergence pass is always staged
+        if (pass > 0 && !last) realign_columns(f);  // as for a handle's fixed-count projection
         f.s_lr = f.s_tb = 1.f;
         f.sweeps = plan[pass];
         f.cdiv = -0.5f * h;

@@ -332,9 +332,11 @@ __device__ __forceinline__ void tile_coords(int b, int tx_n, int ty_n, int& tyi,
 // multiples of four floats and the buffers 16-byte aligned (checked by the caller).
 // Flags of a tile's sweep phase.
 constexpr int kSwEdge = 1;    // a domain-edge tile (edge folding in the sweeps)
-constexpr int kSwDirect = 2;  // a direct tile (global <-> registers)
-constexpr int kSwFirst = 4;   // direct: first diffusion pass (add_sources fused)
+constexpr int kSwDirect = 2;  // a direct tile: global -> registers -> global
+constexpr int kSwFirst = 4;   // direct loads: first diffusion pass (add_sources fused)
 constexpr int kSwResid = 8;   // direct: residual partial sums wanted
+constexpr int kSwLoad = 16;   // load global -> registers (an edge tile: masked, then staged store)
+constexpr int kSwDiv = 32;    // direct loads: first pressure pass (divergence of u, v from P.F)
 struct SweepParams {
     int nsweeps, flags, gy0, gx0, rows, cols;
     float s_lr, s_tb, a, dh, dl, rf;
@@ -506,11 +508,14 @@ __device__ __forceinline__ float2 residual_direct(const float2 (&X)[4][4], int e
 // field's buffer. Kept out of line so that the tile body's other live values are saved
 // once around the call instead of competing with the register blocks, and so that
 // staged and direct interior tiles share one copy of the sweep loop.
-// MODE bits: 1 direct tiles, 2 the direct gradient epilogue, 4 the direct residual sums.
+// MODE bits: 1 direct tiles, 2 the direct gradient epilogue, 4 the direct residual sums,
+// 8 direct (masked) loads for edge tiles too (the batch's many small grids are mostly edge
+// tiles; on one large grid the extra code cost more than it saved), 16 direct first
+// pressure passes (the divergence formed in registers).
 // A direct residual tile leaves its thread's partial sums (rnum, rden) in shared memory
 // at resid_slot(), in the exchange buffer the last sweep used (free once every warp has
 // passed the final exchange's barrier).
-constexpr int kModeDirect = 1, kModeGrad = 2, kModeResid = 4;
+constexpr int kModeDirect = 1, kModeGrad = 2, kModeResid = 4, kModeEdgeLoad = 8, kModeDiv = 16;
 template <int NW>
 __device__ __forceinline__ int resid_slot(int xoff, int nsweeps, int tid) {
     return xoff + (((nsweeps & 1) ^ 1) * (2 * NW * kRegionW)) + 2 * tid;
@@ -532,23 +537,119 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
     const int c_lo = P.halo_l - cb, c_hi = P.halo_l + P.tile_w - cb;
     const bool out_cols = c_lo < 4 && c_hi > 0;
     float2 xb[4][4];
-    if ((MODE & kModeDirect) && (P.flags & kSwDirect)) {
+    if ((MODE & kModeDirect) && (P.flags & kSwLoad)) {
         float* const K = S + koff + w * (8 * RW) + 4 * lane;
         float4 t[8], kk[8];
+        if ((MODE & kModeDiv) && (P.flags & kSwDiv)) {
+            // divergence_kernel (fluid_solver_gpu.cu:173-174): div = cdiv*(((uR - uL) + vD) - vU)
+            // on interior cells, zero elsewhere; the starting pressure where the cell is in the
+            // grid (zero without one). u's left/right neighbours of the block's edge columns
+            // come by shuffles, v's rows above and below the block straight from global memory
+            // (a region-border row or column gets a value that only halo cells depend on).
+            const StencilField& Fd = *P.F;
+            const bool edge = (MODE & kModeEdgeLoad) && (P.flags & kSwEdge);
+            const int gc0 = P.gx0 + cb;
+            unsigned cin = 0xFu, cint = 0xFu;
+            if (edge) {
+                cin = cint = 0;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) t[i] = __ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch));
-#pragma unroll
-        for (int i = 0; i < 8; ++i) kk[i] = __ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch));
-        if (P.flags & kSwFirst) {
-            // add_sources_kernel (fluid_solver_gpu.cu:64), fused as compiled: x0 = x + dt*s
+                for (int q = 0; q < 4; ++q) {
+                    cin |= (unsigned)(gc0 + q >= 0 && gc0 + q < P.cols) << q;
+                    cint |= (unsigned)(gc0 + q >= 1 && gc0 + q <= P.cols - 2) << q;
+                }
+            }
+            auto masked = [](float4 v, unsigned m) {
+                return make_float4((m & 1u) ? v.x : 0.f, (m & 2u) ? v.y : 0.f, (m & 4u) ? v.z : 0.f,
+                                   (m & 8u) ? v.w : 0.f);
+            };
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            auto row_in = [&](int i) {  // grid row of block row i (-1..8) inside the grid
+                const int gr = P.gy0 + rb + i;
+                return !edge || (gr >= 0 && gr < P.rows);
+            };
+            auto load = [&](const float* base, int i) {
+                return (row_in(i) && cin) ? masked(__ldcg(reinterpret_cast<const float4*>(base + (long long)o +
+                                                                                           (long long)i * (long long)pitch)),
+                                                   cin)
+                                          : z;
+            };
+            const float cdiv = Fd.cdiv;
+            float4 vu = load(Fd.x2, -1), vc = load(Fd.x2, 0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
-                t[i].x = __fmaf_rn(P.dt, kk[i].x, t[i].x);
-                t[i].y = __fmaf_rn(P.dt, kk[i].y, t[i].y);
-                t[i].z = __fmaf_rn(P.dt, kk[i].z, t[i].z);
-                t[i].w = __fmaf_rn(P.dt, kk[i].w, t[i].w);
-                kk[i] = t[i];
+                const float4 vd = load(Fd.x2, i + 1);
+                const float4 u = load(Fd.x, i);
+                const float uL = __shfl_up_sync(0xffffffffu, u.w, 1), uR = __shfl_down_sync(0xffffffffu, u.x, 1);
+                const float ul[4] = {uL, u.x, u.y, u.z}, ur[4] = {u.y, u.z, u.w, uR};
+                const float dn[4] = {vd.x, vd.y, vd.z, vd.w}, upv[4] = {vu.x, vu.y, vu.z, vu.w};
+                const int gr = P.gy0 + rb + i;
+                const unsigned mi = (!edge || (gr >= 1 && gr <= P.rows - 2)) ? cint : 0u;
+                float dv[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float sd = __fsub_rn(ur[q], ul[q]);
+                    sd = __fadd_rn(sd, dn[q]);
+                    sd = __fsub_rn(sd, upv[q]);
+                    dv[q] = ((mi >> q) & 1u) ? __fmul_rn(cdiv, sd) : 0.f;
+                }
+                kk[i] = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                vu = vc;
+                vc = vd;
             }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) t[i] = Fd.cst ? load(Fd.cst, i) : z;
+        } else if ((MODE & kModeEdgeLoad) && (P.flags & kSwEdge)) {
+            // an edge tile: the staged loads' masks — the field where the cell is in the grid,
+            // the constant term (and add_sources) where it is an interior cell, zero
+            // elsewhere. The region starts on a multiple of four columns, so a 16-byte
+            // group lies wholly left of the grid, wholly right of it, or inside the
+            // allocated row (the pitch is a multiple of 32 floats).
+            const int gc0 = P.gx0 + cb;
+            unsigned cin = 0, cint = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                cin |= (unsigned)(gc0 + q >= 0 && gc0 + q < P.cols) << q;
+                cint |= (unsigned)(gc0 + q >= 1 && gc0 + q <= P.cols - 2) << q;
+            }
+            auto masked = [](float4 v, unsigned m) {
+                return make_float4((m & 1u) ? v.x : 0.f, (m & 2u) ? v.y : 0.f, (m & 4u) ? v.z : 0.f,
+                                   (m & 8u) ? v.w : 0.f);
+            };
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int gr = P.gy0 + rb + i;
+                const bool rin = gr >= 0 && gr < P.rows, rint = gr >= 1 && gr <= P.rows - 2;
+                t[i] = (rin && cin) ? masked(__ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch)), cin) : z;
+                kk[i] = (rint && cint) ? masked(__ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch)), cint) : z;
+                if (P.flags & kSwFirst) {
+                    // add_sources on interior cells (fluid_solver_gpu.cu:64, fused as compiled)
+                    const unsigned mi = rint ? cint : 0u;
+                    if (mi & 1u) t[i].x = __fmaf_rn(P.dt, kk[i].x, t[i].x);
+                    if (mi & 2u) t[i].y = __fmaf_rn(P.dt, kk[i].y, t[i].y);
+                    if (mi & 4u) t[i].z = __fmaf_rn(P.dt, kk[i].z, t[i].z);
+                    if (mi & 8u) t[i].w = __fmaf_rn(P.dt, kk[i].w, t[i].w);
+                    kk[i] = t[i];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) t[i] = __ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch));
+#pragma unroll
+            for (int i = 0; i < 8; ++i) kk[i] = __ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch));
+            if (P.flags & kSwFirst) {
+                // add_sources_kernel (fluid_solver_gpu.cu:64), fused as compiled: x0 = x + dt*s
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    t[i].x = __fmaf_rn(P.dt, kk[i].x, t[i].x);
+                    t[i].y = __fmaf_rn(P.dt, kk[i].y, t[i].y);
+                    t[i].z = __fmaf_rn(P.dt, kk[i].z, t[i].z);
+                    t[i].w = __fmaf_rn(P.dt, kk[i].w, t[i].w);
+                    kk[i] = t[i];
+                }
+            }
+        }
+        if ((P.flags & (kSwFirst | kSwDiv)) && (P.flags & kSwDirect)) {
             if (P.kout != nullptr && out_cols) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
@@ -601,7 +702,7 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
             }
         }
         const int efin = xoff + (P.nsweeps & 1) * (2 * NW * RW);  // exchange buffer the last sweep did not use
-        if ((MODE & kModeGrad) && P.F != nullptr)
+        if ((MODE & kModeGrad) && P.F != nullptr && P.F->epilogue)
             gradient_direct<NW>(xb, efin, w, lane, o, pitch, r_lo, r_hi, c_lo, c_hi, *P.F);
         if ((MODE & kModeResid) && (P.flags & kSwResid)) {
             const float2 r =
@@ -662,28 +763,31 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
     const int txr = tx < RW - 1 ? tx + 1 : RW - 1;
     const bool edge_cta = gy0 <= 0 || gy0 + RH - 1 >= rows - 1 || gx0 <= 0 || gx0 + RW - 1 >= cols - 1;
 
-    if ((MODE & kModeDirect) && !edge_cta && (!resid || (MODE & kModeResid)) && kind != PASS_PRESSURE_FIRST &&
-        F.sweeps > 0 && ((MODE & kModeGrad) || !F.epilogue) &&
+    // direct loads: a region starting on a multiple of four columns, 16-byte rows and buffers
+    const bool aligned16 =
+        (MODE & kModeDirect) && F.sweeps > 0 && (kind != PASS_PRESSURE_FIRST || (MODE & kModeDiv)) &&
         (((gx0 | F.pitch) & 3) == 0) &&
-        ((reinterpret_cast<uintptr_t>(xin) | reinterpret_cast<uintptr_t>(F.x2) |
-          reinterpret_cast<uintptr_t>(F.cst) | reinterpret_cast<uintptr_t>(yout) |
-          reinterpret_cast<uintptr_t>(F.cst_out) | reinterpret_cast<uintptr_t>(F.u_in) |
-          reinterpret_cast<uintptr_t>(F.v_in) | reinterpret_cast<uintptr_t>(F.u_out) |
-          reinterpret_cast<uintptr_t>(F.v_out)) & 15) == 0) {
-        const bool first = kind == PASS_DIFFUSE_FIRST;
-        SweepParams P = {F.sweeps, kSwDirect | (first ? kSwFirst : 0) | (resid ? kSwResid : 0), gy0, gx0, rows, cols,
-                         F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        ((reinterpret_cast<uintptr_t>(xin) | reinterpret_cast<uintptr_t>(F.x2) | reinterpret_cast<uintptr_t>(F.cst) |
+          reinterpret_cast<uintptr_t>(yout) | reinterpret_cast<uintptr_t>(F.cst_out) |
+          reinterpret_cast<uintptr_t>(F.u_in) | reinterpret_cast<uintptr_t>(F.v_in) |
+          reinterpret_cast<uintptr_t>(F.u_out) | reinterpret_cast<uintptr_t>(F.v_out)) & 15) == 0;
+    const bool first = kind == PASS_DIFFUSE_FIRST;
+    const bool divp = kind == PASS_PRESSURE_FIRST;
+    if (aligned16 && !edge_cta && (!resid || (MODE & kModeResid)) && ((MODE & kModeGrad) || !F.epilogue)) {
+        SweepParams P = {F.sweeps,
+                         kSwLoad | kSwDirect | (first ? kSwFirst : 0) | (divp ? kSwDiv : 0) | (resid ? kSwResid : 0),
+                         gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
         P.x = xin;
         P.k = first ? F.x2 : F.cst;
         P.y = yout;
-        P.kout = first ? F.cst_out : nullptr;
+        P.kout = (first || divp) ? F.cst_out : nullptr;
         P.pitch = F.pitch;
         P.halo = H;
         P.halo_l = HL;
         P.tile_h = F.tile_h;
         P.tile_w = F.tile_w;
         P.dt = F.dt;
-        P.F = (!DIFF && F.epilogue) ? &F : nullptr;
+        P.F = (!DIFF && (F.epilogue || divp)) ? &F : nullptr;
         sweep_phase<DIFF, NW, MODE>(0, RH * RW, P);
         if ((MODE & kModeResid) && resid) {
             const float2 r = *reinterpret_cast<const float2*>(
@@ -717,62 +821,73 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
                                                                          // only masked rows are dereferenced)
 
     // ------------------------------------------------------------------ load
-    // The field goes to S + co and its constant term to S + no, row by row.
-    if (kind == PASS_PRESSURE_FIRST) {
-        // divergence_kernel (fluid_solver_gpu.cu:173-174) on the region, from u, v
-        // staged in the two shared buffers.
+    // Edge tiles with aligned regions load straight into the sweeps' registers (masked, in
+    // sweep_phase) and finish below like staged tiles; the rest load here: the field goes
+    // to S + co and its constant term to S + no, row by row.
+    const bool dload = (MODE & kModeEdgeLoad) && aligned16 && edge_cta;
+    if (!dload) {
+        if (kind == PASS_PRESSURE_FIRST) {
+            // divergence_kernel (fluid_solver_gpu.cu:173-174) on the region, from u, v
+            // staged in the two shared buffers.
 #pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const bool in = (m_in >> i) & 1u;
-            const size_t o = o0 + (size_t)i * pitch;
-            S[co + (r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
-            S[no + (r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
+            for (int i = 0; i < SR; ++i) {
+                const bool in = (m_in >> i) & 1u;
+                const size_t o = o0 + (size_t)i * pitch;
+                S[co + (r0 + i) * RW + tx] = in ? __ldcg(xin + o) : 0.f;
+                S[no + (r0 + i) * RW + tx] = in ? __ldcg(F.x2 + o) : 0.f;
+            }
+            __syncthreads();
+            const float cdiv = F.cdiv;
+            float kc[SR];
+#pragma unroll
+            for (int i = 0; i < SR; ++i) {
+                const int r = r0 + i;
+                const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
+                float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
+                s = __fadd_rn(s, S[no + rd * RW + tx]);
+                s = __fsub_rn(s, S[no + ru * RW + tx]);
+                kc[i] = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
+            }
+            __syncthreads();
+            const float* __restrict__ cst = F.cst;  // starting pressure (null = zero)
+#pragma unroll
+            for (int i = 0; i < SR; ++i) {
+                S[co + (r0 + i) * RW + tx] =
+                    (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
+                KREF(i) = kc[i];
+            }
+        } else if (kind == PASS_DIFFUSE_FIRST) {
+            // add_sources_kernel (fluid_solver_gpu.cu:64) fused into the load
+            const float dt = F.dt;
+#pragma unroll 8
+            for (int i = 0; i < SR; ++i) {
+                const size_t o = o0 + (size_t)i * pitch;
+                float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
+                if ((m_int >> i) & 1u) x = __fmaf_rn(dt, __ldcg(F.x2 + o), x);  // fused, as compiled
+                S[co + (r0 + i) * RW + tx] = x;
+                KREF(i) = x;
+            }
+        } else {
+#pragma unroll 8
+            for (int i = 0; i < SR; ++i) {
+                const size_t o = o0 + (size_t)i * pitch;
+                S[co + (r0 + i) * RW + tx] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
+                KREF(i) = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
+            }
         }
         __syncthreads();
-        const float cdiv = F.cdiv;
-        float kc[SR];
-#pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            const int r = r0 + i;
-            const int ru = r > 0 ? r - 1 : 0, rd = r < RH - 1 ? r + 1 : RH - 1;
-            float s = __fsub_rn(S[co + r * RW + txr], S[co + r * RW + txl]);
-            s = __fadd_rn(s, S[no + rd * RW + tx]);
-            s = __fsub_rn(s, S[no + ru * RW + tx]);
-            kc[i] = ((m_int >> i) & 1u) ? __fmul_rn(cdiv, s) : 0.f;
-        }
-        __syncthreads();
-        const float* __restrict__ cst = F.cst;  // starting pressure (null = zero)
-#pragma unroll
-        for (int i = 0; i < SR; ++i) {
-            S[co + (r0 + i) * RW + tx] =
-                (cst != nullptr && ((m_in >> i) & 1u)) ? __ldcg(cst + o0 + (size_t)i * pitch) : 0.f;
-            KREF(i) = kc[i];
-        }
-    } else if (kind == PASS_DIFFUSE_FIRST) {
-        // add_sources_kernel (fluid_solver_gpu.cu:64) fused into the load
-        const float dt = F.dt;
-#pragma unroll 8
-        for (int i = 0; i < SR; ++i) {
-            const size_t o = o0 + (size_t)i * pitch;
-            float x = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            if ((m_int >> i) & 1u) x = __fmaf_rn(dt, __ldcg(F.x2 + o), x);  // fused, as compiled
-            S[co + (r0 + i) * RW + tx] = x;
-            KREF(i) = x;
-        }
-    } else {
-#pragma unroll 8
-        for (int i = 0; i < SR; ++i) {
-            const size_t o = o0 + (size_t)i * pitch;
-            S[co + (r0 + i) * RW + tx] = ((m_in >> i) & 1u) ? __ldcg(xin + o) : 0.f;
-            KREF(i) = ((m_int >> i) & 1u) ? __ldcg(F.cst + o) : 0.f;
-        }
     }
-    __syncthreads();
 
     // ------------------------------------------------------------------ sweeps
     if (F.sweeps > 0) {
-        SweepParams P = {F.sweeps, edge_cta ? kSwEdge : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
-        P.F = nullptr;
+        SweepParams P = {F.sweeps,
+                         (edge_cta ? kSwEdge : 0) | (dload ? kSwLoad | (first ? kSwFirst : 0) | (divp ? kSwDiv : 0) : 0),
+                         gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        P.x = xin;
+        P.k = first ? F.x2 : F.cst;
+        P.pitch = F.pitch;
+        P.dt = F.dt;
+        P.F = (dload && divp) ? &F : nullptr;
         sweep_phase<DIFF, NW, MODE>(co, no, P);
         if (edge_cta) {
             fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
@@ -951,7 +1066,7 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
     while (f + 1 < L.nfields && b >= L.f[f + 1].tile_begin) ++f;
     const StencilField& F = L.f[f];
     float rn = 0.f, rd = 0.f;
-    process_tile<TY, SRB, DIFF>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
+    process_tile<TY, SRB, DIFF, kModeDirect | kModeGrad | kModeDiv>(F, b - F.tile_begin, F.x, F.y, false, rn, rd);
 }
 
 // One pass over a device-resident table of fields (a batch of grids of uneven size):
@@ -971,7 +1086,8 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
         reinterpret_cast<int*>(&sF)[tid] = __ldg(reinterpret_cast<const int*>(tab + f) + tid);
     __syncthreads();
     float rn = 0.f, rd = 0.f;
-    process_tile<TY, SRB, DIFF>(sF, t - __ldg(prefix + f), sF.x, sF.y, false, rn, rd);
+    process_tile<TY, SRB, DIFF, kModeDirect | kModeGrad | kModeEdgeLoad | kModeDiv>(sF, t - __ldg(prefix + f), sF.x,
+                                                                                    sF.y, false, rn, rd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1074,21 +1190,28 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
         const StencilField& F = cur < 0 ? P.first : P.mid;
         const float* x = cur < 0 ? F.x : P.p[cur];
         const int dst = cur < 0 ? 0 : cur ^ 1;
+        // the residual is formed and tested every second pass (and on the last one allowed):
+        // a pass without it skips the residual sums and the reduction, and a solve runs at
+        // most one pass beyond the one that met the target
+        const bool check = (pass & 1) || pass + 1 >= P.max_passes;
         float rn = 0.f, rd = 0.f;
 #pragma unroll 1
         for (int t = blockIdx.x; t < ntiles; t += G)
-            pressure_tile<TY, SRB>(F, t, x, P.p[dst], true, rn, rd);
+            pressure_tile<TY, SRB>(F, t, x, P.p[dst], check, rn, rd);
         double a = rn, b = rd;
-        block_sum2(a, b);
         double* part = P.partials + (size_t)(pass & 1) * 2 * G;
-        if (tid == 0) {
-            part[2 * blockIdx.x] = a;
-            part[2 * blockIdx.x + 1] = b;
+        if (check) {
+            block_sum2(a, b);
+            if (tid == 0) {
+                part[2 * blockIdx.x] = a;
+                part[2 * blockIdx.x + 1] = b;
+            }
         }
         ok = grid_barrier(P.ctrl, G, limit);
         passes++;
         cur = dst;
         if (!ok) break;
+        if (!check) continue;
         // every CTA sums all partials in the same order, so all agree on the outcome
         a = 0.0;
         b = 0.0;

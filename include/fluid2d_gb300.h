@@ -77,7 +77,9 @@ typedef struct fs_config {
     int use_graph;             /* 1: replay each step as a captured CUDA graph */
     int device;                /* CUDA device ordinal, -1 = the calling thread's current device */
     int warm_start;            /* FS_WARM_ZERO or FS_WARM_PREVIOUS */
-    float pressure_tolerance;  /* > 0: run the pressure solve to this relative residual */
+    float pressure_tolerance;  /* > 0: run the pressure solve to this relative residual (tested
+                                  after every second pass of sweeps_per_pass sweeps and after
+                                  the last pass the cap allows) */
     int pressure_max_iterations; /* iteration cap when pressure_tolerance > 0 */
     int check_finite;          /* 1: flag NaN/Inf in the step's outputs (FS_ERR_NONFINITE) */
     int capture;               /* 1: keep each projection's divergence and starting pressure
@@ -92,7 +94,8 @@ typedef struct fs_config {
     int learned_defect;        /* FS_WARM_LEARNED with a residual target, steps driven from the host:
                                   1 (default) = mixed-precision defect correction (the pressure
                                   kept as two FP32 parts, each cycle solving for a correction of
-                                  the FP64-formed residual); 0 = corrections of the FP32 pressure */
+                                  the residual of their sum, formed in double-float arithmetic);
+                                  0 = corrections of the FP32 pressure */
 } fs_config;
 
 typedef struct fs_stats {
