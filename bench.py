@@ -591,7 +591,7 @@ def run_gauss_seidel(a):
     the GPU (FS_METHOD_GAUSS_SEIDEL): by default on its own CPU-runnable case, 130x130
     (N=128) with 4 density and 4 velocity sources, dt 0.1, rates 1e-4; with --gs-size N
     (N > 128) on the N^2 vortex field of the main workload at 20/20 sweeps (800: the
-    reference app's grid, 2048: the benchmark's; the tiled form above 232). Device-resident
+    reference app's grid, 2048: the benchmark's; the tiled form above 232 interior cells, 234 with the boundary). Device-resident
     steps (value), the reference-style host round trip per step (e2e), the oracle's
     single-thread restatement of the host solver (cpu_baseline, a bounded sample), and a
     bit-for-bit check of the state after the timed steps."""

@@ -1033,7 +1033,7 @@ int check_flags(fs_solver* s) {
         }
     }
     if (s->net_ready && s->net.err) {
-        // a tensor-core wait of the network's convolutions gave up (conv3x3_tc_kernel):
+        // a tensor-core wait of the network gave up (conv3x3_tc_kernel, net_infer32_kernel):
         // stop using the network until fs_set_network loads it again
         int h = 0;
         CK(cudaMemcpyAsync(&h, s->net.err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
