@@ -54,8 +54,8 @@ class fs_stats(C.Structure):
                 ("nonfinite", C.c_int), ("learned_used", C.c_longlong), ("learned_fallback", C.c_longlong)]
 
 
-FS_NUM_KINDS = 5
-KIND_NAMES = ("stencil", "splat", "finish", "advect", "memset")
+FS_NUM_KINDS = 6
+KIND_NAMES = ("stencil", "splat", "finish", "advect", "memset", "gradient")
 
 
 class fs_kernel_times(C.Structure):

@@ -72,14 +72,16 @@ struct fs_batch {
     struct Lane {
         std::vector<int> grids;
         std::vector<Pass> passes;
-        size_t job_off[3] = {}, jprefix_off[3] = {}, jmap_off[3] = {};
-        int job_blocks[3] = {};
+        // ops 0-2: splat, finish, velocity backtrace; 3, 4: the gradient pass of projection 1, 2
+        size_t job_off[5] = {}, jprefix_off[5] = {}, jmap_off[5] = {};
+        int job_blocks[5] = {};
         cudaStream_t stream = nullptr;
         cudaEvent_t done = nullptr;
     };
     std::vector<Lane> lanes;
     cudaEvent_t fork = nullptr;
     int n_diffuse = 0, n_project = 0;
+    bool split = false;  // projections end with a separate gradient launch
     void* d_plan = nullptr;
     size_t d_plan_bytes = 0;
     StencilField* d_tab = nullptr;
@@ -111,6 +113,10 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
     const std::vector<int> pplan = plan_passes(b->cfg.pressure_iterations, K);
     b->n_diffuse = (int)dplan.size();
     b->n_project = (int)pplan.size();
+    // multi-pass projections end with an ordinary pass and a separate gradient launch (the
+    // fused gradient epilogue's loads and stores made the last pass ~1.6x a middle one)
+    const bool split = b->n_project >= 2;
+    b->split = split;
     const int dkinds[3][5] = {{K_ST_D, K_SRC_D, K_X0_D, K_PP_D0, K_PP_D1},
                               {K_ST_U, K_SRC_U, K_X0_U, K_PP_U0, K_PP_U1},
                               {K_ST_V, K_SRC_V, K_X0_V, K_PP_V0, K_PP_V1}};
@@ -163,7 +169,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 for (int g : L.grids) {
                     StencilField f{};
                     field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows,
-                                   pplan[pass] + (last ? 1 : 0));
+                                   pplan[pass] + (last && !split ? 1 : 0));
                     realign_columns(f);
                     const float h = grid_spacing(b->rows[g], b->cols[g]);
                     f.s_lr = f.s_tb = 1.f;
@@ -182,8 +188,8 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                         f.x = b->fld(K_P0 + ((pass - 1) & 1), g);
                         f.cst = b->fld(K_DIV, g);
                     }
-                    f.y = last ? nullptr : b->fld(K_P0 + (pass & 1), g);
-                    if (last) {
+                    f.y = last && !split ? nullptr : b->fld(K_P0 + (pass & 1), g);
+                    if (last && !split) {
                         f.epilogue = 1;
                         f.u_in = uin;
                         f.v_in = vin;
@@ -202,8 +208,9 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 L.passes.push_back(P);
             }
         }
-        // ---- advection jobs: splat, finish, velocity backtrace
-        for (int op = 0; op < 3; ++op) {
+        // ---- advection jobs: splat, finish, velocity backtrace; with multi-pass
+        // projections, the gradient subtract of each projection (gradient_batch_kernel)
+        for (int op = 0; op < (split ? 5 : 3); ++op) {
             L.job_off[op] = b->h_jobs.size();
             L.jprefix_off[op] = b->h_jprefix.size();
             L.jmap_off[op] = b->h_map.size();
@@ -221,11 +228,19 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                 } else if (op == 1) {
                     J.in0 = b->fld(K_ACC, g);
                     J.out0 = b->fld(K_ST_D, g);
-                } else {
+                } else if (op == 2) {
                     J.in0 = b->fld(K_ST_U, g);
                     J.in1 = b->fld(K_ST_V, g);
                     J.out0 = b->fld(K_VEL_U, g);
                     J.out1 = b->fld(K_VEL_V, g);
+                } else {
+                    // the last pass's pressure; the velocity the projection started from
+                    J.A.h = grid_spacing(b->rows[g], b->cols[g]);
+                    J.in0 = b->fld(K_P0 + ((b->n_project - 1) & 1), g);
+                    J.in1 = op == 3 ? b->fld(K_PP_U0 + dlast, g) : b->fld(K_VEL_U, g);
+                    J.in2 = op == 3 ? b->fld(K_PP_V0 + dlast, g) : b->fld(K_VEL_V, g);
+                    J.out0 = b->fld(K_ST_U, g);
+                    J.out1 = b->fld(K_ST_V, g);
                 }
                 b->h_jprefix.push_back(blocks);
                 const int nb = advect_batch_blocks(b->rows[g], b->cols[g]);
@@ -286,13 +301,21 @@ int enqueue_lane(fs_batch* b, const fs_batch::Lane& L, int& launches) {
     FS_CK(launch_advect_batch(1, b->d_jobs + L.job_off[1], b->d_jprefix + L.jprefix_off[1],
                               b->d_map + L.jmap_off[1], L.job_blocks[1], nf, st));
     launches += 2;
+    auto gradient = [&](int op) {
+        if (!b->split) return cudaSuccess;
+        launches++;
+        return launch_gradient_batch(b->d_jobs + L.job_off[op], b->d_jprefix + L.jprefix_off[op],
+                                     b->d_map + L.jmap_off[op], L.job_blocks[op], nf, st);
+    };
     for (int k = 0; k < b->n_project; ++k)
         if ((rc = enqueue_pass(b, L.passes[pi++], st, launches)) != FS_OK) return rc;
+    FS_CK(gradient(3));
     FS_CK(launch_advect_batch(2, b->d_jobs + L.job_off[2], b->d_jprefix + L.jprefix_off[2],
                               b->d_map + L.jmap_off[2], L.job_blocks[2], nullptr, st));
     launches++;
     for (int k = 0; k < b->n_project; ++k)
         if ((rc = enqueue_pass(b, L.passes[pi++], st, launches)) != FS_OK) return rc;
+    FS_CK(gradient(4));
     return FS_OK;
 }
 
@@ -492,7 +515,7 @@ int fs_batch_step(fs_batch* b, float diffusion_rate, float viscosity, float dt, 
             FS_CK(cudaGraphInstantiate(&b->gexec, g, 0));
         } else {
             // stencil passes + three advection launches, per lane
-            launches = (int)b->lanes.size() * (b->n_diffuse + 2 * b->n_project + 3);
+            launches = (int)b->lanes.size() * (b->n_diffuse + 2 * b->n_project + 3 + (b->split ? 2 : 0));
         }
         b->launches_per_step = launches;
         b->graph_valid = true;

@@ -109,6 +109,7 @@ struct AdvectArgs {
     int rows, cols, pitch;
     float dt0;          // sqrt(rows*cols)*dt (fluid_solver_gpu.cu:334)
     float xmax, ymax;   // cols-1.5f, rows-1.5f
+    float h;            // gradient jobs: 1/sqrt(rows*cols) (fluid_solver_gpu.cu:367)
 };
 
 // One grid's work in a batched advection launch. Splat: in0 = d0, in1 = u, in2 = v,
@@ -156,6 +157,14 @@ int record_error(int code, const char* msg);
 // Launchers (stencil.cu, advect.cu).
 cudaError_t stencil_prepare();
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st);
+// remove_p and the reflecting fills of u and v from a final pressure p whose edges are
+// filled (the last pass of a multi-pass projection stores it): u_out, v_out on every cell.
+cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out, int rows,
+                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st);
+// The same over a batch's grids in one launch (blocks as launch_advect_batch's; a job's
+// in0 = p, in1 = u_in, in2 = v_in, out0 = u_out, out1 = v_out, A.h the grid spacing).
+cudaError_t launch_gradient_batch(const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
+                                  int* nonfinite, cudaStream_t st);
 int stencil_max_halo(int tile_rows);
 // Co-resident CTAs of the persistent pressure solve on the current device.
 cudaError_t pressure_solve_max_blocks(int tile_rows, int* blocks);

@@ -543,28 +543,11 @@ int capture_div(fs_solver* s, int slot) {
 // iteration cap is reached, then the gradient subtract (see pressure_solve_kernel).
 int enqueue_fin_pass(fs_solver* s, const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out,
                      Counter& cnt) {
-    StencilLaunch L{};
-    L.nfields = 1;
-    StencilField& f = L.f[0];
-    set_geometry(f, s, 1);
-    f.s_lr = f.s_tb = 1.f;
-    f.sweeps = 0;
-    f.h = grid_h(s->rows, s->cols);
-    f.kind = PASS_PRESSURE;
-    f.x = p;
-    f.cst = s->div;
-    f.y = nullptr;
-    f.epilogue = 1;
-    f.u_in = u_in;
-    f.v_in = v_in;
-    f.u_out = u_out;
-    f.v_out = v_out;
-    f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
     PROF_BEGIN(s);
-    CK(launch_stencil(L, s->tile_rows, s->stream));
-    PROF_END(s, FS_KIND_STENCIL, interior_cells(s) * 28.0);  // read p, u, v (+div); write u, v
+    CK(launch_gradient(p, u_in, v_in, u_out, v_out, s->rows, s->cols, s->pitch, grid_h(s->rows, s->cols),
+                       s->cfg.check_finite ? s->flags : nullptr, s->stream));
+    PROF_END(s, FS_KIND_GRADIENT, interior_cells(s) * 20.0);  // read p, u, v; write u, v
     cnt.launches++;
-    cnt.passes++;
     return FS_OK;
 }
 
@@ -795,21 +778,29 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
     const float* pin = nullptr;
     int rc = projection_start(s, u_in, v_in, slot, cnt, &pin);
     if (rc != FS_OK) return rc;
+    // A single pass fuses the gradient subtract into its epilogue. With more passes the
+    // last is an ordinary pass that stores the final pressure (edges filled) and a separate
+    // bandwidth-bound launch subtracts the gradient (gradient_kernel): the epilogue's loads
+    // and stores, issued behind the sweeps of each tile, had made that pass twice as long
+    // as a middle one (60 against 29 us at 2048^2).
+    const bool split = m >= 2;
+    float* pfinal = nullptr;
     for (int pass = 0; pass < m; ++pass) {
         const bool last = pass == m - 1;
+        const bool fused = last && !split;
         StencilLaunch L{};
         L.nfields = 1;
         StencilField& f = L.f[0];
-        set_geometry(f, s, plan[pass] + (last ? 1 : 0));
-        // middle passes only: the last one's gradient epilogue measured faster staged than
-        // on a realigned tiling (a 9-halo at depth 8), and the first pass's tiling is aligned
-        if (pass > 0 && !last) realign_columns(f);
+        set_geometry(f, s, plan[pass] + (fused ? 1 : 0));
+        if (pass > 0) realign_columns(f);  // the first pass's tiling is aligned at depth 8
         f.s_lr = f.s_tb = 1.f;
         f.sweeps = plan[pass];
         f.cdiv = -0.5f * h;
         f.h = h;
         float* pout = s->p[pass & 1];
-        if (last) pout = warm ? (m == 1 ? s->p[0] : s->pwarm[slot]) : nullptr;
+        if (last && split && warm) pout = s->pwarm[slot];
+        if (fused) pout = warm ? s->p[0] : nullptr;
+        if (last) pfinal = pout;
         if (pass == 0) {
             f.kind = PASS_PRESSURE_FIRST;
             f.x = u_in;
@@ -822,7 +813,7 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
             f.cst = s->div;
         }
         f.y = pout;
-        if (last) {
+        if (fused) {
             f.epilogue = 1;
             f.u_in = u_in;
             f.v_in = v_in;
@@ -832,17 +823,25 @@ int enqueue_project(fs_solver* s, const float* u_in, const float* v_in, float* u
         }
         // 12 B/cell per sweep (read p and div, write p), + 12 divergence, + 20 gradient;
         // the pass itself reads p and div (first: u and v, and p when warm) and writes p
-        // (first: and div; last: u and v instead of p)
+        // (first: and div; a fused last pass: u and v instead of p)
         const double bytes =
-            interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0) + (last ? 20.0 : 0.0));
+            interior_cells(s) * (12.0 * plan[pass] + (pass == 0 ? 12.0 : 0.0) + (fused ? 20.0 : 0.0));
         const double pass_bytes =
-            interior_cells(s) * ((pass == 0 ? 8.0 + (pin ? 4.0 : 0.0) + 4.0 : 8.0) + (last ? 16.0 : 4.0));
+            interior_cells(s) * ((pass == 0 ? 8.0 + (pin ? 4.0 : 0.0) + 4.0 : 8.0) + (fused ? 16.0 : 4.0));
         PROF_BEGIN(s);
         CK(launch_stencil(L, s->tile_rows, s->stream));
         PROF_END_PASS(s, s->stream, FS_KIND_STENCIL, bytes, pass_bytes);
         cnt.launches++;
         cnt.passes++;
         if (pass == 0 && (rc = capture_div(s, slot)) != FS_OK) return rc;
+    }
+    if (split) {
+        // read p, u, v; write u, v
+        PROF_BEGIN(s);
+        CK(launch_gradient(pfinal, u_in, v_in, u_out, v_out, s->rows, s->cols, s->pitch, h,
+                           s->cfg.check_finite ? s->flags : nullptr, s->stream));
+        PROF_END_PASS(s, s->stream, FS_KIND_GRADIENT, interior_cells(s) * 20.0, interior_cells(s) * 20.0);
+        cnt.launches++;
     }
     if (warm && m == 1) {
         CK(cudaMemcpyAsync(s->pwarm[slot], s->p[0], s->field_floats * sizeof(float), cudaMemcpyDeviceToDevice,

@@ -1056,6 +1056,118 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 #undef KREF
 #undef XREF
 
+// Gradient subtract and reflecting fills as a separate pass, from a final pressure p whose
+// edge cells are already filled: remove_p_kernel (fluid_solver_gpu.cu:202-203) on interior
+// cells, then set_boundary_opposite_horizontal(u) / _vertical(v) (fluid_solver_gpu.cu:
+// 402-403): an edge cell takes its inner neighbour's new value, negated for the normal
+// component; corners keep their input value. The same operations, in the same order, as
+// the fused epilogue of the last stencil pass, one cell per thread (a bandwidth-bound
+// pass: p, u, v read, u, v written).
+__device__ __forceinline__ void gradient_cell(const float* __restrict__ p, const float* __restrict__ u_in,
+                                              const float* __restrict__ v_in, int i, int j, int rows, int cols,
+                                              size_t pitch, float h, float rh, float& un, float& vn) {
+    const bool ri = i >= 1 && i <= rows - 2, ci = j >= 1 && j <= cols - 2;
+    const size_t o = (size_t)i * pitch + j;
+    if (!ri && !ci) {
+        un = __ldg(u_in + o);
+        vn = __ldg(v_in + o);
+        return;
+    }
+    int ii = i, jj = j;
+    float su = 1.f, sv = 1.f;
+    if (!ci) {  // left / right edge
+        jj = (j == 0) ? 1 : cols - 2;
+        su = -1.f;
+    } else if (!ri) {  // top / bottom edge
+        ii = (i == 0) ? 1 : rows - 2;
+        sv = -1.f;
+    }
+    const size_t q = (size_t)ii * pitch + jj;
+    const float gu = div_by(__fmul_rn(0.5f, __fsub_rn(__ldg(p + q + 1), __ldg(p + q - 1))), h, rh);
+    const float gv = div_by(__fmul_rn(0.5f, __fsub_rn(__ldg(p + q + pitch), __ldg(p + q - pitch))), h, rh);
+    un = su * __fsub_rn(__ldg(u_in + q), gu);
+    vn = sv * __fsub_rn(__ldg(v_in + q), gv);
+}
+
+// One thread per four consecutive cells of a row: interior groups with 16-byte loads and
+// stores (p's row and its rows above and below, two more p values at the group's ends),
+// groups touching an edge cell per cell.
+__global__ void __launch_bounds__(256) gradient_kernel(const float* __restrict__ p, const float* __restrict__ u_in,
+                                                       const float* __restrict__ v_in, float* __restrict__ u_out,
+                                                       float* __restrict__ v_out, int rows, int cols, int pitch,
+                                                       float h, int* nonfinite) {
+    const int j0 = 4 * (blockIdx.x * 32 + threadIdx.x), i = blockIdx.y * 8 + threadIdx.y;
+    if (i >= rows || j0 >= cols) return;
+    const size_t P = (size_t)pitch;
+    const size_t o = (size_t)i * P + j0;
+    const float rh = __frcp_rn(h);
+    float un[4], vn[4];
+    int n = 4;
+    if (i >= 1 && i <= rows - 2 && j0 >= 1 && j0 + 3 <= cols - 2) {
+        const float4 pc = __ldg(reinterpret_cast<const float4*>(p + o));
+        const float4 pu = __ldg(reinterpret_cast<const float4*>(p + o - P));
+        const float4 pd = __ldg(reinterpret_cast<const float4*>(p + o + P));
+        const float4 u4 = __ldg(reinterpret_cast<const float4*>(u_in + o));
+        const float4 v4 = __ldg(reinterpret_cast<const float4*>(v_in + o));
+        const float pl0 = __ldg(p + o - 1), pr3 = __ldg(p + o + 4);
+        const float pcv[6] = {pl0, pc.x, pc.y, pc.z, pc.w, pr3};
+        const float puv[4] = {pu.x, pu.y, pu.z, pu.w}, pdv[4] = {pd.x, pd.y, pd.z, pd.w};
+        const float uv[4] = {u4.x, u4.y, u4.z, u4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float gu = div_by(__fmul_rn(0.5f, __fsub_rn(pcv[k + 2], pcv[k])), h, rh);
+            const float gv = div_by(__fmul_rn(0.5f, __fsub_rn(pdv[k], puv[k])), h, rh);
+            un[k] = __fsub_rn(uv[k], gu);
+            vn[k] = __fsub_rn(vv[k], gv);
+        }
+        *reinterpret_cast<float4*>(u_out + o) = make_float4(un[0], un[1], un[2], un[3]);
+        *reinterpret_cast<float4*>(v_out + o) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+    } else {
+        n = min(4, cols - j0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k >= n) break;
+            gradient_cell(p, u_in, v_in, i, j0 + k, rows, cols, P, h, rh, un[k], vn[k]);
+            u_out[o + k] = un[k];
+            v_out[o + k] = vn[k];
+        }
+    }
+    if (nonfinite) {
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < n) bad |= !(isfinite(un[k]) && isfinite(vn[k]));
+        if (bad) atomicOr(nonfinite, 1);
+    }
+}
+
+// Batched form: blocks of 32 x 8 threads over 32 x 32 cells of one grid, numbered grid by
+// grid (prefix[g] = first block of grid g, block_job[b] = grid of block b).
+__global__ void __launch_bounds__(256) gradient_batch_kernel(const AdvectJob* __restrict__ jobs,
+                                                             const int* __restrict__ prefix,
+                                                             const int* __restrict__ block_job, int* nonfinite) {
+    const int b = blockIdx.x;
+    const int g = __ldg(block_job + b);
+    const AdvectJob& J = jobs[g];
+    const int lb = b - __ldg(prefix + g);
+    const int bx = (J.A.cols + 31) / 32;
+    const int j = (lb % bx) * 32 + threadIdx.x;
+    const float h = J.A.h, rh = __frcp_rn(h);
+    int bad = 0;
+#pragma unroll
+    for (int r = 0; r < 32; r += 8) {
+        const int i = (lb / bx) * 32 + r + threadIdx.y;
+        if (i >= J.A.rows || j >= J.A.cols) continue;
+        float un, vn;
+        gradient_cell(J.in0, J.in1, J.in2, i, j, J.A.rows, J.A.cols, (size_t)J.A.pitch, h, rh, un, vn);
+        const size_t o = (size_t)i * J.A.pitch + j;
+        J.out0[o] = un;
+        J.out1[o] = vn;
+        bad |= !(isfinite(un) && isfinite(vn));
+    }
+    if (bad && nonfinite) atomicOr(nonfinite, 1);
+}
+
 // One launch = one pass over the tiles of up to kMaxStencilFields fields.
 template <int TY, int SRB, bool DIFF>
 __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
@@ -1334,6 +1446,24 @@ cudaError_t stencil_prepare() {
     cudaError_t e = prepare_variant<2, 8>();
     if (e == cudaSuccess) e = prepare_variant<4, 8>();
     return e;
+}
+
+cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out, int rows,
+                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st) {
+    if (pitch % 4 != 0 || ((reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(u_in) |
+                            reinterpret_cast<uintptr_t>(v_in) | reinterpret_cast<uintptr_t>(u_out) |
+                            reinterpret_cast<uintptr_t>(v_out)) & 15) != 0)
+        return cudaErrorInvalidValue;  // the handles' fields are 128-byte aligned rows
+    const dim3 grid(((cols + 3) / 4 + 31) / 32, (rows + 7) / 8);
+    gradient_kernel<<<grid, dim3(32, 8), 0, st>>>(p, u_in, v_in, u_out, v_out, rows, cols, pitch, h, nonfinite);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_batch(const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
+                                  int* nonfinite, cudaStream_t st) {
+    if (nblocks <= 0) return cudaSuccess;
+    gradient_batch_kernel<<<nblocks, dim3(32, 8), 0, st>>>(jobs, prefix, block_job, nonfinite);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t st) {

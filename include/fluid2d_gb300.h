@@ -296,7 +296,8 @@ FS_API int fs_batch_stream(fs_batch* b, void** stream);
 #define FS_KIND_FINISH 2    /* density fill + smoothing */
 #define FS_KIND_ADVECT 3    /* velocity backtrace advection */
 #define FS_KIND_MEMSET 4    /* accumulator clear (a memset node, not a kernel) */
-#define FS_NUM_KINDS 5
+#define FS_KIND_GRADIENT 5  /* gradient subtract + reflecting fills after a multi-pass projection */
+#define FS_NUM_KINDS 6
 typedef struct fs_kernel_times {
     int launches[FS_NUM_KINDS];
     double ms[FS_NUM_KINDS];
