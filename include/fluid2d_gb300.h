@@ -89,7 +89,7 @@ typedef struct fs_config {
                                   corrections per projection, each followed by Jacobi sweeps;
                                   0 = as many as pressure_max_iterations allows. Steps stop at
                                   convergence (read on the host after each segment). */
-    int learned_cycle_iterations; /* Jacobi sweeps after each correction; 0 = 128 */
+    int learned_cycle_iterations; /* Jacobi sweeps after each correction; 0 = 256 */
     int learned_grid;          /* coarse grid side of the network, 32 or 64; 0 = 32 */
     int learned_defect;        /* FS_WARM_LEARNED with a residual target, steps driven from the host:
                                   1 (default) = mixed-precision defect correction (the pressure
