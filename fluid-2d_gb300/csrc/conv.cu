@@ -236,6 +236,7 @@ constexpr int kWgBbytes = kC * kWgK * 2;       // 4096
 constexpr int kWgStage = kWgAbytes + kWgBbytes;
 constexpr int kWgSmem = 2 * kWgStage + 64;
 constexpr int kWgOut = 289;                // rows of the partial result (288 weights + bias)
+constexpr int kWgThreads = 256;            // 8 warps; two CTAs per SM (shared memory and TMEM allow it)
 
 struct WgradArgs {
     const __nv_bfloat16* x;   // layer input NHWC (as in ConvArgs, `up` for nearest-upsampled)
@@ -264,7 +265,7 @@ __device__ __forceinline__ void transpose8x8_b16(const uint4 (&in)[8], uint4 (&o
     }
 }
 
-__global__ void __launch_bounds__(128) wgrad_tc_kernel(const WgradArgs P) {
+__global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(const WgradArgs P) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kWgStage);  // one per buffer
     uint32_t* s_taddr = reinterpret_cast<uint32_t*>(sm + 2 * kWgStage + 32);
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(128) wgrad_tc_kernel(const WgradArgs P) {
     // rest zero; the staging below never writes them
     for (int b = 0; b < 2; ++b) {
         uint4* z = reinterpret_cast<uint4*>(sm + b * kWgStage + 36 * 8 * 128);
-        for (int e = tid; e < 12 * 8 * 8; e += 128) {
+        for (int e = tid; e < 12 * 8 * 8; e += kWgThreads) {
             const bool ones = e < 8 * 8 && (e & 7) == 0;  // core matrices (36, pg), row 0
             z[e] = ones ? make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u) : make_uint4(0, 0, 0, 0);
         }
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(128) wgrad_tc_kernel(const WgradArgs P) {
         }
         const long c0 = pbeg + (long)s * kWgK;
         // items: 288 of A (tap t, channel group cg, pixel group pg), 32 of B (cg, pg)
-        for (int q = tid; q < 320; q += 128) {
+        for (int q = tid; q < 320; q += kWgThreads) {
             uint4 in[8], out[8];
             uint8_t* dst;
             if (q < 288) {
@@ -380,12 +381,13 @@ __global__ void __launch_bounds__(128) wgrad_tc_kernel(const WgradArgs P) {
     tc::fence_after_sync();
     if (ok && all_arrived) {
         float* out = P.work + (size_t)blockIdx.x * kWgOut * kC;
+        // warp w reads tensor-memory lanes 32*(w%4).. of the tiles g = w/4, w/4 + 2
 #pragma unroll 1
-        for (int g = 0; g < 3; ++g) {
-            const int f = g * 128 + warp * 32 + lane;
+        for (int g = warp >> 2; g < 3; g += kWgThreads / 128) {
+            const int f = g * 128 + (warp & 3) * 32 + lane;
             float v[32];
             if (nchunks > 0) {
-                tc::tmem_ld_32x32(taddr + ((uint32_t)(warp * 32) << 16) + g * 32, v);
+                tc::tmem_ld_32x32(taddr + ((uint32_t)((warp & 3) * 32) << 16) + g * 32, v);
             } else {
 #pragma unroll
                 for (int c = 0; c < 32; ++c) v[c] = 0.f;
@@ -726,7 +728,7 @@ extern "C" long long fs_net_weight_grad_tc_work_floats(int H, int W) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
-    return (long long)sms * kWgOut * kC;
+    return 2LL * sms * kWgOut * kC;
 }
 
 extern "C" int fs_net_weight_grad_tc(const void* dzb, const void* x, float* dw, float* db, float* work,
@@ -738,6 +740,7 @@ extern "C" int fs_net_weight_grad_tc(const void* dzb, const void* x, float* dw, 
         return record_error(FS_ERR_ARG, "fs_net_weight_grad_tc: upsampled output must be even");
     const long long per_block = (long long)kWgOut * kC;
     const long long max_blocks = work_floats / per_block;
+    // two CTAs per SM
     if (max_blocks < 1) return record_error(FS_ERR_ARG, "fs_net_weight_grad_tc: workspace too small");
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -748,10 +751,10 @@ extern "C" int fs_net_weight_grad_tc(const void* dzb, const void* x, float* dw, 
             return record_error(FS_ERR_CUDA, "fs_net_weight_grad_tc: smem attribute");
         configured |= 1ull << (dev & 63);
     }
-    // one CTA per SM at most, each over a whole number of 64-pixel chunks
+    // two CTAs per SM at most, each over a whole number of 64-pixel chunks
     const long npix = (long)H * W;
     const long chunks = (npix + kWgK - 1) / kWgK;
-    long nb = std::min<long>({(long)sms, chunks, (long)max_blocks});
+    long nb = std::min<long>({2L * sms, chunks, (long)max_blocks});
     const long per = ((chunks + nb - 1) / nb) * kWgK;
     nb = (npix + per - 1) / per;
     WgradArgs P;
@@ -765,7 +768,7 @@ extern "C" int fs_net_weight_grad_tc(const void* dzb, const void* x, float* dw, 
     P.per = (int)per;
     P.err = err;
     cudaStream_t st = (cudaStream_t)stream;
-    wgrad_tc_kernel<<<(unsigned)nb, 128, kWgSmem, st>>>(P);
+    wgrad_tc_kernel<<<(unsigned)nb, kWgThreads, kWgSmem, st>>>(P);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return record_error(FS_ERR_CUDA, "fs_net_weight_grad_tc: launch failed");
     wgrad_reduce_kernel<<<(kWgOut * kC + 255) / 256, 256, 0, st>>>(work, (int)nb, dw, db);

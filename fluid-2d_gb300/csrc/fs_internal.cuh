@@ -77,21 +77,22 @@ struct SolveCtrl {
     int error;      // 1: a grid barrier gave up waiting (FS_ERR_TIMEOUT)
     int passes;     // passes executed (each runs `sweeps` Jacobi sweeps)
     int converged;  // 1: relative residual <= tol
-    int pad;
+    int cur;        // index in PressureSolve::p of the final pressure (whole solves)
     double residual;  // relative residual after the last executed pass
 };
 
 // A whole pressure solve run to a residual target by one persistent cooperative
 // launch: `first` (divergence fused) then `mid` passes until the relative residual
-// drops to tol or max_passes ran, then `fin` (zero sweeps: gradient subtract and
-// reflecting fills). Passes ping-pong between p[0] and p[1].
+// drops to tol or max_passes ran. Passes ping-pong between p[0] and p[1]; the launch
+// records which holds the final pressure (ctrl->cur), copies it to p_out when given, and
+// the gradient subtract follows as launch_gradient with that selector.
 //
 // Segment mode (learned corrections): the divergence already exists, `first` is a
 // PASS_PRESSURE field whose x is p_cur and `fin` is unused. The launch does nothing if
 // ctrl->converged is already set; otherwise it runs passes from p_cur until the target
 // or max_passes and copies the final pressure back to p_cur. ctrl->passes accumulates.
 struct PressureSolve {
-    StencilField first, mid, fin;
+    StencilField first, mid;
     float* p[2];
     float* p_out;      // receives the final pressure (warm start); may be null
     double* partials;  // 4 doubles per CTA (residual sums, double-buffered by pass)
@@ -160,7 +161,8 @@ cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t s
 // remove_p and the reflecting fills of u and v from a final pressure p whose edges are
 // filled (the last pass of a multi-pass projection stores it): u_out, v_out on every cell.
 cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out, int rows,
-                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st);
+                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st,
+                            const float* p_alt = nullptr, const int* sel = nullptr);  // p_alt when *sel != 0
 // The same over a batch's grids in one launch (blocks as launch_advect_batch's; a job's
 // in0 = p, in1 = u_in, in2 = v_in, out0 = u_out, out1 = v_out, A.h the grid spacing).
 cudaError_t launch_gradient_batch(const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,

@@ -742,19 +742,6 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
     P.first.cst_out = s->div;
     P.mid.kind = PASS_PRESSURE;
     P.mid.cst = s->div;
-    StencilField& f = P.fin;
-    set_geometry(f, s, 1);
-    f.s_lr = f.s_tb = 1.f;
-    f.sweeps = 0;
-    f.h = h;
-    f.kind = PASS_PRESSURE;
-    f.cst = s->div;
-    f.epilogue = 1;
-    f.u_in = u_in;
-    f.v_in = v_in;
-    f.u_out = u_out;
-    f.v_out = v_out;
-    f.nonfinite = s->cfg.check_finite ? s->flags : nullptr;
     P.p[0] = s->p[0];
     P.p[1] = s->p[1];
     P.p_out = warm ? s->pwarm[slot] : nullptr;
@@ -768,7 +755,12 @@ int enqueue_project_to_residual(fs_solver* s, const float* u_in, const float* v_
     PROF_BEGIN(s);
     CK(launch_pressure_solve(P, s->tile_rows, blocks, s->stream));
     PROF_END(s, FS_KIND_STENCIL, 0.0);  // bytes depend on the iteration count reached
-    cnt.launches++;
+    // gradient subtract from the buffer the solve ended in (P.ctrl->cur)
+    PROF_BEGIN(s);
+    CK(launch_gradient(s->p[0], u_in, v_in, u_out, v_out, s->rows, s->cols, s->pitch, h,
+                       s->cfg.check_finite ? s->flags : nullptr, s->stream, s->p[1], &P.ctrl->cur));
+    PROF_END(s, FS_KIND_GRADIENT, interior_cells(s) * 20.0);  // read p, u, v; write u, v
+    cnt.launches += 2;
     cnt.passes++;
     return capture_div(s, slot);
 }

@@ -1092,12 +1092,13 @@ __device__ __forceinline__ void gradient_cell(const float* __restrict__ p, const
 // One thread per four consecutive cells of a row: interior groups with 16-byte loads and
 // stores (p's row and its rows above and below, two more p values at the group's ends),
 // groups touching an edge cell per cell.
-__global__ void __launch_bounds__(256) gradient_kernel(const float* __restrict__ p, const float* __restrict__ u_in,
+__global__ void __launch_bounds__(256) gradient_kernel(const float* p0, const float* __restrict__ u_in,
                                                        const float* __restrict__ v_in, float* __restrict__ u_out,
                                                        float* __restrict__ v_out, int rows, int cols, int pitch,
-                                                       float h, int* nonfinite) {
+                                                       float h, int* nonfinite, const float* p_alt, const int* sel) {
     const int j0 = 4 * (blockIdx.x * 32 + threadIdx.x), i = blockIdx.y * 8 + threadIdx.y;
     if (i >= rows || j0 >= cols) return;
+    const float* __restrict__ p = (sel != nullptr && __ldcg(sel) != 0) ? p_alt : p0;
     const size_t P = (size_t)pitch;
     const size_t o = (size_t)i * P + j0;
     const float rh = __frcp_rn(h);
@@ -1343,12 +1344,15 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
             const long n4 = (long)P.mid.rows * P.mid.pitch / 4;
             for (long e = (long)blockIdx.x * nt + tid; e < n4; e += (long)G * nt) dst[e] = __ldcg(src + e);
         } else {
-            // gradient subtract + reflecting fills from the final pressure
-            const int nfin = P.fin.tiles_x * P.fin.tiles_y;
-            float rn = 0.f, rd = 0.f;
-#pragma unroll 1
-            for (int t = blockIdx.x; t < nfin; t += G)
-                pressure_tile<TY, SRB>(P.fin, t, P.p[cur], P.p_out, false, rn, rd);
+            // the final pressure: which buffer holds it (the gradient pass that follows
+            // reads it there), and a copy for the next step's warm start
+            if (blockIdx.x == 0 && tid == 0) P.ctrl->cur = cur;
+            if (P.p_out) {
+                const float4* src = reinterpret_cast<const float4*>(P.p[cur]);
+                float4* dst = reinterpret_cast<float4*>(P.p_out);
+                const long n4 = (long)P.mid.rows * P.mid.pitch / 4;
+                for (long e = (long)blockIdx.x * nt + tid; e < n4; e += (long)G * nt) dst[e] = __ldcg(src + e);
+            }
         }
     }
     if (blockIdx.x == 0 && tid == 0) {
@@ -1449,13 +1453,15 @@ cudaError_t stencil_prepare() {
 }
 
 cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out, int rows,
-                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st) {
-    if (pitch % 4 != 0 || ((reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(u_in) |
-                            reinterpret_cast<uintptr_t>(v_in) | reinterpret_cast<uintptr_t>(u_out) |
-                            reinterpret_cast<uintptr_t>(v_out)) & 15) != 0)
+                            int cols, int pitch, float h, int* nonfinite, cudaStream_t st, const float* p_alt,
+                            const int* sel) {
+    if (pitch % 4 != 0 || ((reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(p_alt) |
+                            reinterpret_cast<uintptr_t>(u_in) | reinterpret_cast<uintptr_t>(v_in) |
+                            reinterpret_cast<uintptr_t>(u_out) | reinterpret_cast<uintptr_t>(v_out)) & 15) != 0)
         return cudaErrorInvalidValue;  // the handles' fields are 128-byte aligned rows
     const dim3 grid(((cols + 3) / 4 + 31) / 32, (rows + 7) / 8);
-    gradient_kernel<<<grid, dim3(32, 8), 0, st>>>(p, u_in, v_in, u_out, v_out, rows, cols, pitch, h, nonfinite);
+    gradient_kernel<<<grid, dim3(32, 8), 0, st>>>(p, u_in, v_in, u_out, v_out, rows, cols, pitch, h, nonfinite, p_alt,
+                                                  sel);
     return cudaGetLastError();
 }
 
