@@ -1456,13 +1456,13 @@ int fs_set_barrier_poll_limit(fs_solver* s, unsigned polls) {
 
 namespace {
 
-int launch_repack(fs_solver* s, float* const* stage, float* const* dst, int count) {
+int launch_repack(fs_solver* s, float* const* stage, float* const* dst, int count, cudaStream_t st = nullptr) {
     Repack6 R{};
     for (int k = 0; k < count; ++k) {
         R.src[k] = stage[k];
         R.dst[k] = dst[k];
     }
-    repack_kernel<<<dim3(152 * 2, count), 256, 0, s->stream>>>(R, s->rows, s->cols, s->pitch);
+    repack_kernel<<<dim3(152 * 2, count), 256, 0, st ? st : s->stream>>>(R, s->rows, s->cols, s->pitch);
     CK(cudaGetLastError());
     return FS_OK;
 }
@@ -1488,23 +1488,31 @@ int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const
     // uploads begin after the handle's earlier work, which may still read the scratch
     CK(cudaEventRecord(s->xev[0], s->stream));
     CK(cudaStreamWaitEvent(up, s->xev[0], 0));
-    for (int k = 0; k < 2; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
-    CK(cudaEventRecord(s->xev[1], up));
+    // The velocity and its sources go up first: their diffusion and the two projections
+    // are the step's critical path. The density and its source follow while the velocity
+    // diffuses, and the density's diffusion and advection run on the side stream.
+    for (int k = 2; k < 6; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
+    CK(cudaEventRecord(s->xev[2], up));
     Counter cnt;
     int rc;
-    CK(cudaStreamWaitEvent(s->stream, s->xev[1], 0));
-    if ((rc = launch_repack(s, stage, dst, 2)) != FS_OK) return rc;
+    CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
+    if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
+    CK(cudaEventRecord(s->side_ev[0], s->stream));  // the state holds the step's initial velocity
     const int fd = F_D, fuv[2] = {F_U, F_V};
     const float rd = diff, ruv[2] = {visc, visc};
     float *dif_d, *dif_uv[2];
-    if ((rc = enqueue_diffuse(s, &fd, 1, &rd, dt, &dif_d, cnt)) != FS_OK) return rc;
-    // issued after the density work so that a pageable (host-blocking) copy still overlaps it
-    for (int k = 2; k < 6; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
-    CK(cudaEventRecord(s->xev[2], up));
-    CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
-    if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
     if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
-    if ((rc = fork_density(s, dif_d, diff, dt, false, cnt)) != FS_OK) return rc;
+    // issued after the velocity's diffusion so that a pageable (host-blocking) copy still
+    // overlaps it
+    for (int k = 0; k < 2; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
+    CK(cudaEventRecord(s->xev[1], up));
+    CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
+    CK(cudaStreamWaitEvent(s->side, s->xev[1], 0));
+    if ((rc = launch_repack(s, stage, dst, 2, s->side)) != FS_OK) return rc;
+    if ((rc = enqueue_diffuse(s, &fd, 1, &rd, dt, &dif_d, cnt, s->side)) != FS_OK) return rc;
+    if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, s->side)) != FS_OK)
+        return rc;
+    CK(cudaEventRecord(s->side_ev[1], s->side));  // joined before the second projection
     CK(cudaEventRecord(s->xev[3], s->side));
     if ((rc = enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt)) != FS_OK) return rc;
     // the density download is issued after the velocity work for the same reason
