@@ -154,7 +154,7 @@ struct fs_solver {
     // fs_solve_host on large grids: upload and download streams beside `stream`, and
     // the events that order them (created by the first such call)
     cudaStream_t xfer[2] = {};
-    cudaEvent_t xev[5] = {};
+    cudaEvent_t xev[6] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool graph_valid = false;
@@ -1467,8 +1467,8 @@ int launch_repack(fs_solver* s, float* const* stage, float* const* dst, int coun
     return FS_OK;
 }
 
-// One Jacobi step on host grids with the copies overlapped: density and its source go up
-// first and density diffuses while the four velocity grids are still on their way; the
+// One Jacobi step on host grids with the copies overlapped: the six grids go up as three
+// (field, source) pairs and each field diffuses while the next pair is on its way; the
 // new density goes down while the velocity is projected and advected. Each field sees
 // the same kernels as in enqueue_step, so the results are those of upload + step +
 // download. host: density, u, v, density source, u source, v source; out: density, u, v.
@@ -1488,40 +1488,38 @@ int solve_host_overlapped(fs_solver* s, const float* const host[6], float* const
     // uploads begin after the handle's earlier work, which may still read the scratch
     CK(cudaEventRecord(s->xev[0], s->stream));
     CK(cudaStreamWaitEvent(up, s->xev[0], 0));
-    // The velocity and its sources go up first: their diffusion and the two projections
-    // are the step's critical path. The density and its source follow while the velocity
-    // diffuses, and the density's diffusion and advection run on the side stream.
-    for (int k = 2; k < 6; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
-    CK(cudaEventRecord(s->xev[2], up));
+    // Three pairs go up one after another — density and its source, then u and its source,
+    // then v and its source — and each field diffuses as soon as its pair has landed, so
+    // the GPU works while the rest is still on the link (a one-field diffusion takes about
+    // as long as the next pair's upload). The density's advection, which needs the step's
+    // initial u and v, runs on the side stream beside the first projection.
+    const int pairs[3][2] = {{0, 1}, {2, 4}, {3, 5}};  // stage indices: field, source
+    const int fields[3] = {F_D, F_U, F_V};
+    const float rates[3] = {diff, visc, visc};
+    float* dif[3] = {};
     Counter cnt;
     int rc;
-    CK(cudaStreamWaitEvent(s->stream, s->xev[2], 0));
-    if ((rc = launch_repack(s, stage + 2, dst + 2, 4)) != FS_OK) return rc;
-    CK(cudaEventRecord(s->side_ev[0], s->stream));  // the state holds the step's initial velocity
-    const int fd = F_D, fuv[2] = {F_U, F_V};
-    const float rd = diff, ruv[2] = {visc, visc};
-    float *dif_d, *dif_uv[2];
-    if ((rc = enqueue_diffuse(s, fuv, 2, ruv, dt, dif_uv, cnt)) != FS_OK) return rc;
-    // issued after the velocity's diffusion so that a pageable (host-blocking) copy still
-    // overlaps it
-    for (int k = 0; k < 2; ++k) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
-    CK(cudaEventRecord(s->xev[1], up));
-    CK(cudaStreamWaitEvent(s->side, s->side_ev[0], 0));
-    CK(cudaStreamWaitEvent(s->side, s->xev[1], 0));
-    if ((rc = launch_repack(s, stage, dst, 2, s->side)) != FS_OK) return rc;
-    if ((rc = enqueue_diffuse(s, &fd, 1, &rd, dt, &dif_d, cnt, s->side)) != FS_OK) return rc;
-    if ((rc = enqueue_advect_density(s, dif_d, s->st[F_D], s->st[F_U], s->st[F_V], dt, cnt, s->side)) != FS_OK)
-        return rc;
-    CK(cudaEventRecord(s->side_ev[1], s->side));  // joined before the second projection
-    CK(cudaEventRecord(s->xev[3], s->side));
+    for (int q = 0; q < 3; ++q) {
+        for (int k : pairs[q]) CK(cudaMemcpyAsync(stage[k], from[k], bytes, cudaMemcpyHostToDevice, up));
+        CK(cudaEventRecord(s->xev[1 + q], up));
+        CK(cudaStreamWaitEvent(s->stream, s->xev[1 + q], 0));
+        float* const st2[2] = {stage[pairs[q][0]], stage[pairs[q][1]]};
+        float* const ds2[2] = {dst[pairs[q][0]], dst[pairs[q][1]]};
+        if ((rc = launch_repack(s, st2, ds2, 2)) != FS_OK) return rc;
+        if ((rc = enqueue_diffuse(s, &fields[q], 1, &rates[q], dt, &dif[q], cnt)) != FS_OK) return rc;
+    }
+    if ((rc = fork_density(s, dif[0], diff, dt, false, cnt)) != FS_OK) return rc;
+    CK(cudaEventRecord(s->xev[4], s->side));
+    float* dif_uv[2] = {dif[1], dif[2]};
     if ((rc = enqueue_velocity_tail(s, dif_uv[0], dif_uv[1], dt, cnt)) != FS_OK) return rc;
-    // the density download is issued after the velocity work for the same reason
-    CK(cudaStreamWaitEvent(down, s->xev[3], 0));
+    // the density download is issued after the velocity work so that a pageable
+    // (host-blocking) copy still overlaps it
+    CK(cudaStreamWaitEvent(down, s->xev[4], 0));
     if ((rc = copy_out(s, out[0], s->st[F_D], down)) != FS_OK) return rc;
-    CK(cudaEventRecord(s->xev[4], down));
+    CK(cudaEventRecord(s->xev[5], down));
     if ((rc = copy_out(s, out[1], s->st[F_U])) || (rc = copy_out(s, out[2], s->st[F_V]))) return rc;
-    CK(cudaStreamWaitEvent(s->stream, s->xev[4], 0));
-    cnt.launches += 2;
+    CK(cudaStreamWaitEvent(s->stream, s->xev[5], 0));
+    cnt.launches += 3;  // the repacks
     s->launches_per_step = cnt.launches;
     s->passes_per_step = cnt.passes;
     s->stats.kernel_launches += cnt.launches;
