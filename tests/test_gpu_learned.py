@@ -49,7 +49,8 @@ def test_forward_and_gradients_match_cpu_reference(fluid):
     y0 = y.cpu().numpy().reshape(B, G, G, 32)[..., 0]
     yr = y_ref.detach().numpy()[..., 0]
     assert np.abs(y0 - yr).max() <= 2e-2 * np.abs(yr).max()
-    assert abs(float(lg) - float(loss)) <= 2e-2 * float(loss)
+    loss = float(loss.detach())
+    assert abs(float(lg) - loss) <= 2e-2 * loss
     live = Lm.frozen_mask() == 0
     cos = np.dot(grad[live], g_ref[live]) / (np.linalg.norm(grad[live]) * np.linalg.norm(g_ref[live]))
     assert cos > 0.999, cos
