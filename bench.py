@@ -99,7 +99,8 @@ def parse():
 # interior cell and field by one depth-8 pass at 2048^2, and the unit that bounds the pass
 NCU_DRAM_BYTES_PER_CELL_FIELD_PASS = 8.2
 NCU_BINDING = ("instruction issue and latency: 2 CTAs of 8 warps per SM at 128 registers (24 % of the warp "
-               "slots); ncu on a 2048^2 middle pressure pass: issue active 40 %, DRAM 15 %, L1/shared 51 %")
+               "slots); ncu on a 2048^2 middle pressure pass: issue active 39 %, DRAM 15 %, L1/shared 48 %, "
+               "largest stall instruction fetch")
 
 
 def dist_env():
