@@ -243,7 +243,8 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                     J.out1 = b->fld(K_ST_V, g);
                 }
                 b->h_jprefix.push_back(blocks);
-                const int nb = advect_batch_blocks(b->rows[g], b->cols[g]);
+                const int nb = op >= 3 ? gradient_batch_blocks(b->rows[g], b->cols[g])
+                                       : advect_batch_blocks(b->rows[g], b->cols[g]);
                 blocks += nb;
                 b->h_map.insert(b->h_map.end(), nb, jobs++);
                 b->h_jobs.push_back(J);

@@ -163,8 +163,10 @@ cudaError_t launch_stencil(const StencilLaunch& L, int tile_rows, cudaStream_t s
 cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in, float* u_out, float* v_out, int rows,
                             int cols, int pitch, float h, int* nonfinite, cudaStream_t st,
                             const float* p_alt = nullptr, const int* sel = nullptr);  // p_alt when *sel != 0
-// The same over a batch's grids in one launch (blocks as launch_advect_batch's; a job's
-// in0 = p, in1 = u_in, in2 = v_in, out0 = u_out, out1 = v_out, A.h the grid spacing).
+// The same over a batch's grids in one launch (gradient_batch_blocks(rows, cols) blocks per
+// grid, numbered as launch_advect_batch's; a job's in0 = p, in1 = u_in, in2 = v_in,
+// out0 = u_out, out1 = v_out, A.h the grid spacing; rows 16-byte aligned).
+int gradient_batch_blocks(int rows, int cols);
 cudaError_t launch_gradient_batch(const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                   int* nonfinite, cudaStream_t st);
 int stencil_max_halo(int tile_rows);

@@ -1089,19 +1089,16 @@ __device__ __forceinline__ void gradient_cell(const float* __restrict__ p, const
     vn = sv * __fsub_rn(__ldg(v_in + q), gv);
 }
 
-// One thread per four consecutive cells of a row: interior groups with 16-byte loads and
-// stores (p's row and its rows above and below, two more p values at the group's ends),
-// groups touching an edge cell per cell.
-__global__ void __launch_bounds__(256) gradient_kernel(const float* p0, const float* __restrict__ u_in,
-                                                       const float* __restrict__ v_in, float* __restrict__ u_out,
-                                                       float* __restrict__ v_out, int rows, int cols, int pitch,
-                                                       float h, int* nonfinite, const float* p_alt, const int* sel) {
-    const int j0 = 4 * (blockIdx.x * 32 + threadIdx.x), i = blockIdx.y * 8 + threadIdx.y;
-    if (i >= rows || j0 >= cols) return;
-    const float* __restrict__ p = (sel != nullptr && __ldcg(sel) != 0) ? p_alt : p0;
-    const size_t P = (size_t)pitch;
+// Four consecutive cells (i, j0 .. j0 + 3) of the gradient subtract: an interior group
+// with 16-byte loads and stores (p's row and its rows above and below, two more p values
+// at the group's ends), a group touching an edge cell per cell. Requires the rows 16-byte
+// aligned (pitch a multiple of four, buffers 16-byte aligned). Returns true when an
+// output is NaN or Inf.
+__device__ __forceinline__ bool gradient_group(const float* __restrict__ p, const float* __restrict__ u_in,
+                                               const float* __restrict__ v_in, float* __restrict__ u_out,
+                                               float* __restrict__ v_out, int i, int j0, int rows, int cols,
+                                               size_t P, float h, float rh) {
     const size_t o = (size_t)i * P + j0;
-    const float rh = __frcp_rn(h);
     float un[4], vn[4];
     int n = 4;
     if (i >= 1 && i <= rows - 2 && j0 >= 1 && j0 + 3 <= cols - 2) {
@@ -1133,17 +1130,30 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float* p0, const fl
             v_out[o + k] = vn[k];
         }
     }
-    if (nonfinite) {
-        bool bad = false;
+    bool bad = false;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < n) bad |= !(isfinite(un[k]) && isfinite(vn[k]));
-        if (bad) atomicOr(nonfinite, 1);
-    }
+    for (int k = 0; k < 4; ++k)
+        if (k < n) bad |= !(isfinite(un[k]) && isfinite(vn[k]));
+    return bad;
 }
 
-// Batched form: blocks of 32 x 8 threads over 32 x 32 cells of one grid, numbered grid by
-// grid (prefix[g] = first block of grid g, block_job[b] = grid of block b).
+// One thread per four consecutive cells of a row (gradient_group).
+__global__ void __launch_bounds__(256) gradient_kernel(const float* p0, const float* __restrict__ u_in,
+                                                       const float* __restrict__ v_in, float* __restrict__ u_out,
+                                                       float* __restrict__ v_out, int rows, int cols, int pitch,
+                                                       float h, int* nonfinite, const float* p_alt, const int* sel) {
+    const int j0 = 4 * (blockIdx.x * 32 + threadIdx.x), i = blockIdx.y * 8 + threadIdx.y;
+    if (i >= rows || j0 >= cols) return;
+    const float* __restrict__ p = (sel != nullptr && __ldcg(sel) != 0) ? p_alt : p0;
+    const bool bad = gradient_group(p, u_in, v_in, u_out, v_out, i, j0, rows, cols, (size_t)pitch, h, __frcp_rn(h));
+    if (bad && nonfinite) atomicOr(nonfinite, 1);
+}
+
+// Batched form: blocks of 32 x 8 threads over 128 columns x kGradBatchRows rows of one
+// grid (gradient_batch_blocks per grid), numbered grid by grid (prefix[g] = first block of
+// grid g, block_job[b] = grid of block b); each thread takes four cells of a row, as
+// gradient_kernel, in kGradBatchRows / 8 rows.
+constexpr int kGradBatchRows = 32;
 __global__ void __launch_bounds__(256) gradient_batch_kernel(const AdvectJob* __restrict__ jobs,
                                                              const int* __restrict__ prefix,
                                                              const int* __restrict__ block_job, int* nonfinite) {
@@ -1151,20 +1161,16 @@ __global__ void __launch_bounds__(256) gradient_batch_kernel(const AdvectJob* __
     const int g = __ldg(block_job + b);
     const AdvectJob& J = jobs[g];
     const int lb = b - __ldg(prefix + g);
-    const int bx = (J.A.cols + 31) / 32;
-    const int j = (lb % bx) * 32 + threadIdx.x;
+    const int rows = J.A.rows, cols = J.A.cols;
+    const int bx = ((cols + 3) / 4 + 31) / 32;
+    const int j0 = 4 * ((lb % bx) * 32 + threadIdx.x);
     const float h = J.A.h, rh = __frcp_rn(h);
-    int bad = 0;
+    bool bad = false;
 #pragma unroll
-    for (int r = 0; r < 32; r += 8) {
-        const int i = (lb / bx) * 32 + r + threadIdx.y;
-        if (i >= J.A.rows || j >= J.A.cols) continue;
-        float un, vn;
-        gradient_cell(J.in0, J.in1, J.in2, i, j, J.A.rows, J.A.cols, (size_t)J.A.pitch, h, rh, un, vn);
-        const size_t o = (size_t)i * J.A.pitch + j;
-        J.out0[o] = un;
-        J.out1[o] = vn;
-        bad |= !(isfinite(un) && isfinite(vn));
+    for (int r = 0; r < kGradBatchRows; r += 8) {
+        const int i = (lb / bx) * kGradBatchRows + r + threadIdx.y;
+        if (i >= rows || j0 >= cols) continue;
+        bad |= gradient_group(J.in0, J.in1, J.in2, J.out0, J.out1, i, j0, rows, cols, (size_t)J.A.pitch, h, rh);
     }
     if (bad && nonfinite) atomicOr(nonfinite, 1);
 }
@@ -1463,6 +1469,10 @@ cudaError_t launch_gradient(const float* p, const float* u_in, const float* v_in
     gradient_kernel<<<grid, dim3(32, 8), 0, st>>>(p, u_in, v_in, u_out, v_out, rows, cols, pitch, h, nonfinite, p_alt,
                                                   sel);
     return cudaGetLastError();
+}
+
+int gradient_batch_blocks(int rows, int cols) {
+    return (((cols + 3) / 4 + 31) / 32) * ((rows + kGradBatchRows - 1) / kGradBatchRows);
 }
 
 cudaError_t launch_gradient_batch(const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
