@@ -11,12 +11,14 @@ seeded low-frequency noise, no sources. Metric: interior cell-steps per second.
   e2e       the same metric through fs_solve_host() with pinned host buffers: each
             step uploads the state and sources and downloads the state, like the
             reference's fluid_solver_gpu::solve.
-  roofline  stencil kernels (the dominant kind): algorithmic bytes per launch (the
-            per-sweep model 12 B/cell/sweep + fused work) over their CUDA-event time
-            in profiled steps, against the measured HBM copy bandwidth. A profiled step
-            runs its kernels one after another with events between them, so its
-            diffusion passes are the fused three-field launches, where the timed step
-            graph may run the density's passes on a side branch.
+  roofline  stencil kernels (the dominant kind): the bytes each pass must move (every
+            array it reads or writes, once: 12 B per interior cell and field for a
+            middle pass) over the passes' CUDA-event time in a profiled step, against
+            the measured HBM copy bandwidth. The profiled step has the timed graph's
+            launches and streams, with an event around each launch. Beside it: the
+            per-sweep model (12 B per cell and field per sweep, what the reference's
+            one kernel per sweep moves) as model_equivalent_*, DRAM traffic per launch
+            from ncu (traffic, dram_frac) and the resource that binds the pass.
   cpu_baseline  the oracle's Jacobi restatement of the same step (OpenMP, all host
             cores) on a bounded sample.
 
@@ -77,6 +79,9 @@ def parse():
     ap.add_argument("--max-iters", type=int, default=None,
                     help="sweep cap per projection (default: residual 2000, learned 20000, depth 400)")
     ap.add_argument("--count", type=int, default=256)
+    ap.add_argument("--batch-sizes", default="",
+                    help="batch: comma-separated interior sizes, one grid each (default: --count seeded "
+                         "sizes in 64..1024)")
     ap.add_argument("--gs-size", type=int, default=128, help="gauss-seidel: interior cells per side")
     ap.add_argument("--depth-target-steps", type=int, default=0,
                     help="depth: also time coarse-corrected solves that reach --tol, for this many steps")
@@ -683,7 +688,8 @@ def run_batch(a):
 
     build_lib.build()
     kd = kp = 30
-    all_sims = workloads.batch(a.count, seed=4, kd=kd, kp=kp)
+    sizes = [int(x) for x in a.batch_sizes.split(",")] if a.batch_sizes else None
+    all_sims = workloads.batch(a.count, seed=4, kd=kd, kp=kp, sizes=sizes)
     mine = replicas.shard([(w.rows, w.cols) for w in all_sims], world, rank, kd, kp)
     sims = [all_sims[i] for i in mine]
     shapes = [(w.rows, w.cols) for w in sims]
@@ -760,7 +766,9 @@ def run_batch(a):
                 "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_b / a.steps,
                 "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded vortex fields + sources)", "gpu_launches": launches,
-                "config": {"workload": f"batch of {len(all_sims)} grids, N uniform in 64..1024, Kd=Kp=30, dt 0.05",
+                "config": {"workload": (f"batch of {len(all_sims)} grids, N uniform in 64..1024, Kd=Kp=30, dt 0.05"
+                                        if not sizes else
+                                        f"batch of {len(all_sims)} grids, N = {a.batch_sizes}, Kd=Kp=30, dt 0.05"),
                            "interior_cells": total_cells, "rank0_grids": len(sims),
                            "launches_per_step": st["launches_per_step"], "sweeps_per_pass": st["sweeps_per_pass"],
                            "tile_rows": st["tile_rows"], "l2": "flushed between timed steps",

@@ -4,9 +4,10 @@
 // The reference advances one grid per fluid_solver_gpu object, one kernel per sweep
 // (fluid_solver_gpu.cu:222-404). A batch here advances every grid of the batch with
 // the same stage sequence as a single handle, but each sub-step is ONE launch over
-// all grids: the stencil passes walk a device-resident table of per-grid field
-// descriptors (tiles of all grids concatenated, one CTA per tile, a tile -> field
-// map), and the advection stages walk a table of per-grid jobs (a block -> job map).
+// all grids: a stencil pass carries the grids' field descriptors in its launch
+// parameters (tiles of all grids concatenated, one CTA per tile; a pass of more fields
+// than the parameter space holds is split into launches of equal field counts), and the
+// advection stages walk a device table of per-grid jobs (a block -> job map).
 // The grids are dealt to a few lanes (longest-processing-time first, by cells) and each
 // lane runs its own sequence of launches on its own stream, so one lane's small final
 // wave overlaps another lane's work instead of idling the GPU between sub-steps. The
@@ -57,14 +58,13 @@ struct fs_batch {
     float g_diff = 0, g_visc = 0, g_dt = 0;
     int sweeps = 8, tile_rows = 64;
     // host-built plan, mirrored in one device buffer
-    std::vector<StencilField> h_tab;
-    std::vector<int> h_prefix;
+    std::vector<WideLaunch> h_wide;  // stencil launches (descriptors travel as parameters)
     std::vector<AdvectJob> h_jobs;
     std::vector<int> h_jprefix;
-    std::vector<int> h_map;   // tile -> field for every pass, then block -> job for every op
+    std::vector<int> h_map;   // block -> job for every advection op
     struct Pass {
-        size_t tab, prefix, map;  // offsets into the tables
-        int nfields, total;
+        size_t first;  // launches h_wide[first, first + count)
+        int count;
         bool diffuse;
     };
     // one lane: its grids, its passes (diffusion, project 1, project 2) and advection
@@ -84,8 +84,6 @@ struct fs_batch {
     bool split = false;  // projections end with a separate gradient launch
     void* d_plan = nullptr;
     size_t d_plan_bytes = 0;
-    StencilField* d_tab = nullptr;
-    int* d_prefix = nullptr;
     AdvectJob* d_jobs = nullptr;
     int* d_jprefix = nullptr;
     int* d_map = nullptr;
@@ -101,10 +99,36 @@ int fail(int code, const char* msg) { return record_error(code, msg); }
 
 constexpr int kBatchLanes = 4;
 
-// Builds every table of one step for (diff, visc, dt) and uploads them.
+// One stencil pass over the fields fl: ceil(n / kMaxWideFields) launches with as even a
+// share of the fields as possible, each field's tiles numbered from its launch's start.
+fs_batch::Pass add_pass(fs_batch* b, const std::vector<StencilField>& fl, bool diffuse) {
+    const int n = (int)fl.size();
+    const int nl = (n + kMaxWideFields - 1) / kMaxWideFields;
+    fs_batch::Pass P{b->h_wide.size(), nl, diffuse};
+    int f0 = 0;
+    for (int l = 0; l < nl; ++l) {
+        const int cnt = n / nl + (l < n % nl ? 1 : 0);
+        b->h_wide.emplace_back();
+        WideLaunch& W = b->h_wide.back();
+        std::memset(&W, 0, sizeof(W));
+        W.nfields = cnt;
+        int tiles = 0;
+        for (int i = 0; i < cnt; ++i) {
+            W.f[i] = fl[f0 + i];
+            W.f[i].tile_begin = tiles;
+            W.begin[i] = tiles;
+            tiles += W.f[i].tiles_x * W.f[i].tiles_y;
+        }
+        W.begin[cnt] = tiles;
+        f0 += cnt;
+    }
+    return P;
+}
+
+// Builds the launches and job tables of one step for (diff, visc, dt) and uploads the
+// tables.
 int build_plan(fs_batch* b, float diff, float visc, float dt) {
-    b->h_tab.clear();
-    b->h_prefix.clear();
+    b->h_wide.clear();
     b->h_jobs.clear();
     b->h_jprefix.clear();
     b->h_map.clear();
@@ -127,8 +151,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
         L.passes.clear();
         // ---- diffusion passes over the lane's grids x {d, u, v}; add_sources fused in pass 0
         for (size_t pass = 0; pass < dplan.size(); ++pass) {
-            fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, true};
-            int tiles = 0;
+            std::vector<StencilField> fl;
             for (int g : L.grids)
                 for (int q = 0; q < 3; ++q) {
                     StencilField f{};
@@ -150,22 +173,15 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                         f.kind = PASS_DIFFUSE;
                         f.cst = b->fld(k[2], g);
                     }
-                    b->h_prefix.push_back(tiles);
-                    tiles += f.tiles_x * f.tiles_y;
-                    b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
-                    b->h_tab.push_back(f);
-                    P.nfields++;
+                    fl.push_back(f);
                 }
-            b->h_prefix.push_back(tiles);
-            P.total = tiles;
-            L.passes.push_back(P);
+            L.passes.push_back(add_pass(b, fl, true));
         }
         // ---- two projections over the lane's grids (one pressure field each)
         for (int proj = 0; proj < 2; ++proj) {
             for (int pass = 0; pass < b->n_project; ++pass) {
                 const bool last = pass == b->n_project - 1;
-                fs_batch::Pass P{b->h_tab.size(), b->h_prefix.size(), b->h_map.size(), 0, 0, false};
-                int tiles = 0;
+                std::vector<StencilField> fl;
                 for (int g : L.grids) {
                     StencilField f{};
                     field_geometry(f, b->rows[g], b->cols[g], b->pitch[g], b->tile_rows,
@@ -197,15 +213,9 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
                         f.v_out = b->fld(K_ST_V, g);
                         f.nonfinite = b->cfg.check_finite ? b->flags : nullptr;
                     }
-                    b->h_prefix.push_back(tiles);
-                    tiles += f.tiles_x * f.tiles_y;
-                    b->h_map.insert(b->h_map.end(), f.tiles_x * f.tiles_y, P.nfields);
-                    b->h_tab.push_back(f);
-                    P.nfields++;
+                    fl.push_back(f);
                 }
-                b->h_prefix.push_back(tiles);
-                P.total = tiles;
-                L.passes.push_back(P);
+                L.passes.push_back(add_pass(b, fl, false));
             }
         }
         // ---- advection jobs: splat, finish, velocity backtrace; with multi-pass
@@ -254,13 +264,11 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
         }
     }
     // ---- upload (one buffer, tables first)
-    const size_t tab_bytes = b->h_tab.size() * sizeof(StencilField);
-    const size_t pre_bytes = b->h_prefix.size() * sizeof(int);
     const size_t job_bytes = b->h_jobs.size() * sizeof(AdvectJob);
     const size_t jpre_bytes = b->h_jprefix.size() * sizeof(int);
     const size_t map_bytes = b->h_map.size() * sizeof(int);
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t need = up(tab_bytes) + up(pre_bytes) + up(job_bytes) + up(jpre_bytes) + up(map_bytes);
+    const size_t need = up(job_bytes) + up(jpre_bytes) + up(map_bytes);
     if (need > b->d_plan_bytes) {
         if (b->d_plan) cudaFree(b->d_plan);
         b->d_plan = nullptr;
@@ -269,13 +277,9 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
         b->d_plan_bytes = need;
     }
     char* base = static_cast<char*>(b->d_plan);
-    b->d_tab = reinterpret_cast<StencilField*>(base);
-    b->d_prefix = reinterpret_cast<int*>(base + up(tab_bytes));
-    b->d_jobs = reinterpret_cast<AdvectJob*>(base + up(tab_bytes) + up(pre_bytes));
-    b->d_jprefix = reinterpret_cast<int*>(base + up(tab_bytes) + up(pre_bytes) + up(job_bytes));
-    b->d_map = reinterpret_cast<int*>(base + up(tab_bytes) + up(pre_bytes) + up(job_bytes) + up(jpre_bytes));
-    FS_CK(cudaMemcpyAsync(b->d_tab, b->h_tab.data(), tab_bytes, cudaMemcpyHostToDevice, b->stream));
-    FS_CK(cudaMemcpyAsync(b->d_prefix, b->h_prefix.data(), pre_bytes, cudaMemcpyHostToDevice, b->stream));
+    b->d_jobs = reinterpret_cast<AdvectJob*>(base);
+    b->d_jprefix = reinterpret_cast<int*>(base + up(job_bytes));
+    b->d_map = reinterpret_cast<int*>(base + up(job_bytes) + up(jpre_bytes));
     FS_CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs.data(), job_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaMemcpyAsync(b->d_jprefix, b->h_jprefix.data(), jpre_bytes, cudaMemcpyHostToDevice, b->stream));
     FS_CK(cudaMemcpyAsync(b->d_map, b->h_map.data(), map_bytes, cudaMemcpyHostToDevice, b->stream));
@@ -284,9 +288,10 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
 }
 
 int enqueue_pass(fs_batch* b, const fs_batch::Pass& P, cudaStream_t st, int& launches) {
-    FS_CK(launch_stencil_table(b->d_tab + P.tab, b->d_prefix + P.prefix, b->d_map + P.map, P.total, P.diffuse,
-                               b->tile_rows, st));
-    launches++;
+    for (int i = 0; i < P.count; ++i) {
+        FS_CK(launch_stencil_wide(b->h_wide[P.first + i], P.diffuse, b->tile_rows, st));
+        launches++;
+    }
     return FS_OK;
 }
 
@@ -515,8 +520,11 @@ int fs_batch_step(fs_batch* b, float diffusion_rate, float viscosity, float dt, 
             b->graph = g;
             FS_CK(cudaGraphInstantiate(&b->gexec, g, 0));
         } else {
-            // stencil passes + three advection launches, per lane
-            launches = (int)b->lanes.size() * (b->n_diffuse + 2 * b->n_project + 3 + (b->split ? 2 : 0));
+            // stencil launches + three advection launches (+ two gradient launches), per lane
+            for (const fs_batch::Lane& L : b->lanes) {
+                for (const fs_batch::Pass& P : L.passes) launches += P.count;
+                launches += 3 + (b->split ? 2 : 0);
+            }
         }
         b->launches_per_step = launches;
         b->graph_valid = true;

@@ -235,10 +235,17 @@ int advect_batch_blocks(int rows, int cols);
 // covers 32x32 cells; prefix[g] = first block of job g, block_job[b] = job of block b.
 cudaError_t launch_advect_batch(int op, const AdvectJob* jobs, const int* prefix, const int* block_job, int nblocks,
                                 int* nonfinite, cudaStream_t st);
-// Stencil pass over a device table of fields (batched grids); prefix[f] = first tile
-// of field f, tile_field[t] = field of tile t.
-cudaError_t launch_stencil_table(const StencilField* table, const int* prefix, const int* tile_field, int total_tiles,
-                                 bool diffuse, int tile_rows, cudaStream_t st);
+// Stencil pass over many fields of one class (diffusion or pressure) of a batch's grids,
+// the descriptors carried in the launch's parameters (at most 32,764 bytes on this
+// architecture): field f owns the tiles [begin[f], begin[f + 1]) of the launch.
+constexpr int kMaxWideFields = 168;
+struct WideLaunch {
+    int nfields;
+    int begin[kMaxWideFields + 1];
+    StencilField f[kMaxWideFields];
+};
+static_assert(sizeof(WideLaunch) <= 32764, "a launch's parameter space holds 32,764 bytes");
+cudaError_t launch_stencil_wide(const WideLaunch& L, bool diffuse, int tile_rows, cudaStream_t st);
 cudaError_t launch_advect_velocity(const float* u0, const float* v0, float* u, float* v, const AdvectArgs& A,
                                    cudaStream_t st);
 

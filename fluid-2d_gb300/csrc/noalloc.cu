@@ -17,7 +17,8 @@
 //
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (and sets the kernels' shared-memory limit) and caches it for
-// that device. A cudaDeviceReset() on a
+// that device; make that first call before any stream capture begins on the device,
+// since the set-up calls are not stream work. A cudaDeviceReset() on a
 // device releases the array and leaves the cached address stale: calls on that device
 // after a reset are not supported. Every call shares the
 // one array: calls that can overlap on the GPU (different streams, or different host

@@ -157,11 +157,12 @@ def batch_sizes(count=256, seed=4, choices=tuple(range(64, 1025, 64))):
     return [int(x) for x in rng.choice(np.array(choices), size=count)]
 
 
-def batch(count=256, seed=4, kd=30, kp=30, dt=0.05, rate=1e-5):
+def batch(count=256, seed=4, kd=30, kp=30, dt=0.05, rate=1e-5, sizes=None):
     """Independent simulations of uneven size, each with its own vortex field and
-    density sources (vortex count and radii scaled with the grid)."""
+    density sources (vortex count and radii scaled with the grid). `sizes` (interior
+    cells per side, one per grid) replaces the seeded draw of `count` sizes."""
     sims = []
-    for k, N in enumerate(batch_sizes(count, seed)):
+    for k, N in enumerate(sizes if sizes else batch_sizes(count, seed)):
         n = N + 2
         scale = N / 2048.0
         cnt = max(2, int(round(16 * (N / 1024.0) ** 2)))

@@ -326,7 +326,8 @@ FS_API int fs_profile_step(fs_solver* s, float diffusion_rate, float viscosity, 
  * Scratch (divergence and two pressure buffers) lives in a fixed file-scope device
  * array of 3 x FS_NOALLOC_MAX_CELLS floats (12 MiB) that every GPU loading this library
  * holds until process exit; rows * pitch above FS_NOALLOC_MAX_CELLS is rejected with
- * FS_ERR_ARG. The first call on a device looks up that array's address and caches it.
+ * FS_ERR_ARG. The first call on a device looks up that array's address and caches it;
+ * make that first call before any stream capture begins on the device.
  * After cudaDeviceReset() on a device the cached
  * address is stale and further calls on that device are not supported. All calls share
  * the array, so calls that may overlap on the GPU race and must be serialised by the
