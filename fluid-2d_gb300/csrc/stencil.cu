@@ -335,7 +335,7 @@ constexpr int kSwEdge = 1;    // a domain-edge tile (edge folding in the sweeps)
 constexpr int kSwDirect = 2;  // a direct tile: global -> registers -> global
 constexpr int kSwFirst = 4;   // direct loads: first diffusion pass (add_sources fused)
 constexpr int kSwResid = 8;   // direct: residual partial sums wanted
-constexpr int kSwLoad = 16;   // load global -> registers (an edge tile: masked, then staged store)
+constexpr int kSwLoad = 16;   // direct tiles: load global -> registers
 constexpr int kSwDiv = 32;    // direct loads: first pressure pass (divergence of u, v from P.F)
 struct SweepParams {
     int nsweeps, flags, gy0, gx0, rows, cols;
@@ -509,13 +509,13 @@ __device__ __forceinline__ float2 residual_direct(const float2 (&X)[4][4], int e
 // once around the call instead of competing with the register blocks, and so that
 // staged and direct interior tiles share one copy of the sweep loop.
 // MODE bits: 1 direct tiles, 2 the direct gradient epilogue, 4 the direct residual sums,
-// 8 direct (masked) loads for edge tiles too (the batch's many small grids are mostly edge
-// tiles; on one large grid the extra code cost more than it saved), 16 direct first
-// pressure passes (the divergence formed in registers).
+// 16 direct first pressure passes (the divergence formed in registers). Edge tiles are
+// always staged: masked direct loads for them were measured slower, on a large grid and
+// over a batch of small ones alike.
 // A direct residual tile leaves its thread's partial sums (rnum, rden) in shared memory
 // at resid_slot(), in the exchange buffer the last sweep used (free once every warp has
 // passed the final exchange's barrier).
-constexpr int kModeDirect = 1, kModeGrad = 2, kModeResid = 4, kModeEdgeLoad = 8, kModeDiv = 16;
+constexpr int kModeDirect = 1, kModeGrad = 2, kModeResid = 4, kModeDiv = 16;
 template <int NW>
 __device__ __forceinline__ int resid_slot(int xoff, int nsweeps, int tid) {
     return xoff + (((nsweeps & 1) ^ 1) * (2 * NW * kRegionW)) + 2 * tid;
@@ -542,36 +542,15 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
         float4 t[8], kk[8];
         if ((MODE & kModeDiv) && (P.flags & kSwDiv)) {
             // divergence_kernel (fluid_solver_gpu.cu:173-174): div = cdiv*(((uR - uL) + vD) - vU)
-            // on interior cells, zero elsewhere; the starting pressure where the cell is in the
-            // grid (zero without one). u's left/right neighbours of the block's edge columns
-            // come by shuffles, v's rows above and below the block straight from global memory
-            // (a region-border row or column gets a value that only halo cells depend on).
+            // on every cell of the region (a direct tile's region lies inside the grid's
+            // interior); the starting pressure (zero without one). u's left/right neighbours
+            // of the block's edge columns come by shuffles, v's rows above and below the block
+            // straight from global memory (a region-border row or column gets a value that
+            // only halo cells depend on).
             const StencilField& Fd = *P.F;
-            const bool edge = (MODE & kModeEdgeLoad) && (P.flags & kSwEdge);
-            const int gc0 = P.gx0 + cb;
-            unsigned cin = 0xFu, cint = 0xFu;
-            if (edge) {
-                cin = cint = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    cin |= (unsigned)(gc0 + q >= 0 && gc0 + q < P.cols) << q;
-                    cint |= (unsigned)(gc0 + q >= 1 && gc0 + q <= P.cols - 2) << q;
-                }
-            }
-            auto masked = [](float4 v, unsigned m) {
-                return make_float4((m & 1u) ? v.x : 0.f, (m & 2u) ? v.y : 0.f, (m & 4u) ? v.z : 0.f,
-                                   (m & 8u) ? v.w : 0.f);
-            };
             const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            auto row_in = [&](int i) {  // grid row of block row i (-1..8) inside the grid
-                const int gr = P.gy0 + rb + i;
-                return !edge || (gr >= 0 && gr < P.rows);
-            };
             auto load = [&](const float* base, int i) {
-                return (row_in(i) && cin) ? masked(__ldcg(reinterpret_cast<const float4*>(base + (long long)o +
-                                                                                           (long long)i * (long long)pitch)),
-                                                   cin)
-                                          : z;
+                return __ldcg(reinterpret_cast<const float4*>(base + (long long)o + (long long)i * (long long)pitch));
             };
             const float cdiv = Fd.cdiv;
             float4 vu = load(Fd.x2, -1), vc = load(Fd.x2, 0);
@@ -582,15 +561,13 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
                 const float uL = __shfl_up_sync(0xffffffffu, u.w, 1), uR = __shfl_down_sync(0xffffffffu, u.x, 1);
                 const float ul[4] = {uL, u.x, u.y, u.z}, ur[4] = {u.y, u.z, u.w, uR};
                 const float dn[4] = {vd.x, vd.y, vd.z, vd.w}, upv[4] = {vu.x, vu.y, vu.z, vu.w};
-                const int gr = P.gy0 + rb + i;
-                const unsigned mi = (!edge || (gr >= 1 && gr <= P.rows - 2)) ? cint : 0u;
                 float dv[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     float sd = __fsub_rn(ur[q], ul[q]);
                     sd = __fadd_rn(sd, dn[q]);
                     sd = __fsub_rn(sd, upv[q]);
-                    dv[q] = ((mi >> q) & 1u) ? __fmul_rn(cdiv, sd) : 0.f;
+                    dv[q] = __fmul_rn(cdiv, sd);
                 }
                 kk[i] = make_float4(dv[0], dv[1], dv[2], dv[3]);
                 vu = vc;
@@ -598,40 +575,6 @@ __device__ __noinline__ void sweep_phase(int xoff, int koff, const SweepParams P
             }
 #pragma unroll
             for (int i = 0; i < 8; ++i) t[i] = Fd.cst ? load(Fd.cst, i) : z;
-        } else if ((MODE & kModeEdgeLoad) && (P.flags & kSwEdge)) {
-            // an edge tile: the staged loads' masks — the field where the cell is in the grid,
-            // the constant term (and add_sources) where it is an interior cell, zero
-            // elsewhere. The region starts on a multiple of four columns, so a 16-byte
-            // group lies wholly left of the grid, wholly right of it, or inside the
-            // allocated row (the pitch is a multiple of 32 floats).
-            const int gc0 = P.gx0 + cb;
-            unsigned cin = 0, cint = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                cin |= (unsigned)(gc0 + q >= 0 && gc0 + q < P.cols) << q;
-                cint |= (unsigned)(gc0 + q >= 1 && gc0 + q <= P.cols - 2) << q;
-            }
-            auto masked = [](float4 v, unsigned m) {
-                return make_float4((m & 1u) ? v.x : 0.f, (m & 2u) ? v.y : 0.f, (m & 4u) ? v.z : 0.f,
-                                   (m & 8u) ? v.w : 0.f);
-            };
-            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int gr = P.gy0 + rb + i;
-                const bool rin = gr >= 0 && gr < P.rows, rint = gr >= 1 && gr <= P.rows - 2;
-                t[i] = (rin && cin) ? masked(__ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch)), cin) : z;
-                kk[i] = (rint && cint) ? masked(__ldcg(reinterpret_cast<const float4*>(P.k + o + i * pitch)), cint) : z;
-                if (P.flags & kSwFirst) {
-                    // add_sources on interior cells (fluid_solver_gpu.cu:64, fused as compiled)
-                    const unsigned mi = rint ? cint : 0u;
-                    if (mi & 1u) t[i].x = __fmaf_rn(P.dt, kk[i].x, t[i].x);
-                    if (mi & 2u) t[i].y = __fmaf_rn(P.dt, kk[i].y, t[i].y);
-                    if (mi & 4u) t[i].z = __fmaf_rn(P.dt, kk[i].z, t[i].z);
-                    if (mi & 8u) t[i].w = __fmaf_rn(P.dt, kk[i].w, t[i].w);
-                    kk[i] = t[i];
-                }
-            }
         } else {
 #pragma unroll
             for (int i = 0; i < 8; ++i) t[i] = __ldcg(reinterpret_cast<const float4*>(P.x + o + i * pitch));
@@ -821,11 +764,8 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
                                                                          // only masked rows are dereferenced)
 
     // ------------------------------------------------------------------ load
-    // Edge tiles with aligned regions load straight into the sweeps' registers (masked, in
-    // sweep_phase) and finish below like staged tiles; the rest load here: the field goes
-    // to S + co and its constant term to S + no, row by row.
-    const bool dload = (MODE & kModeEdgeLoad) && aligned16 && edge_cta;
-    if (!dload) {
+    // The field goes to S + co and its constant term to S + no, row by row.
+    {
         if (kind == PASS_PRESSURE_FIRST) {
             // divergence_kernel (fluid_solver_gpu.cu:173-174) on the region, from u, v
             // staged in the two shared buffers.
@@ -880,14 +820,11 @@ __device__ __forceinline__ void process_tile(const StencilField& F, int b, const
 
     // ------------------------------------------------------------------ sweeps
     if (F.sweeps > 0) {
-        SweepParams P = {F.sweeps,
-                         (edge_cta ? kSwEdge : 0) | (dload ? kSwLoad | (first ? kSwFirst : 0) | (divp ? kSwDiv : 0) : 0),
-                         gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
+        SweepParams P = {F.sweeps, edge_cta ? kSwEdge : 0, gy0, gx0, rows, cols, F.s_lr, F.s_tb, F.a, F.dh, F.dl, F.rf};
         P.x = xin;
         P.k = first ? F.x2 : F.cst;
         P.pitch = F.pitch;
         P.dt = F.dt;
-        P.F = (dload && divp) ? &F : nullptr;
         sweep_phase<DIFF, NW, MODE>(co, no, P);
         if (edge_cta) {
             fill_edges<SR, RH>(co, r0, tx, txl, txr, g0, gc, rows, cols, F.s_lr, F.s_tb);
