@@ -669,7 +669,8 @@ def run_gauss_seidel(a):
 
 def run_batch(a):
     """256 independent grids, N uniform in {64..1024}, 30/30 sweeps: one fs_batch
-    (one launch per sub-step, graph per step) vs the same grids as 256 handles. Under
+    (one launch per sub-step, graph per step; tiling from the batch autotuner unless
+    --sweeps / --tile-rows fix it) vs the same grids as 256 handles. Under
     torchrun (N > 1) the grids are dealt to ranks by longest-processing-time-first on
     cells x sweeps (replicas.shard), each rank steps its own batch, and the ranks meet
     only at the barriers around the timed region; the value is all ranks' cells over the
@@ -697,10 +698,18 @@ def run_batch(a):
     total_cells = sum(w.interior_cells for w in all_sims)
     w0 = sims[0]
     cfg = dict(diffuse_iterations=kd, pressure_iterations=kp, device=dev, check_finite=0)
-    if a.sweeps:
-        cfg["sweeps_per_pass"] = a.sweeps
-    if a.tile_rows:
-        cfg["tile_rows"] = a.tile_rows
+    cfg_handles = dict(cfg)  # the handles keep their own default tiling rule
+    tuned = None
+    if a.sweeps or a.tile_rows:
+        if a.sweeps:
+            cfg["sweeps_per_pass"] = cfg_handles["sweeps_per_pass"] = a.sweeps
+        if a.tile_rows:
+            cfg["tile_rows"] = cfg_handles["tile_rows"] = a.tile_rows
+    else:
+        # the batch's tiling from its autotuner (whole batch steps per candidate)
+        tuned = pkg.autotune_batch(shapes, w0.diffusion, w0.viscosity, w0.dt, steps=2, **cfg)
+        cfg["sweeps_per_pass"] = tuned["sweeps_per_pass"]
+        cfg["tile_rows"] = tuned["tile_rows"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     b = pkg.Batch(shapes, **cfg)
     for k, w in enumerate(sims):
@@ -743,7 +752,7 @@ def run_batch(a):
         # the same grids as independent handles, stepped one after another per step
         hs = []
         for w in sims:
-            s = pkg.Solver(w.rows, w.cols, **cfg)
+            s = pkg.Solver(w.rows, w.cols, **cfg_handles)
             s.upload(*w.state())
             s.upload_sources(*w.sources())
             s.step(w.diffusion, w.viscosity, w.dt, nsteps=1)
@@ -774,6 +783,8 @@ def run_batch(a):
                            "tile_rows": st["tile_rows"], "l2": "flushed between timed steps",
                            "parallelism": f"grids dealt to {world} rank(s) by LPT on cells x sweeps"},
                 "clocks": clk}
+        if tuned:
+            line["autotuner"] = tuned
         line["batch_wall_clock"] = {"value": total_cells / (batch_wall_ms / 1e3), "ms_per_step": batch_wall_ms,
                                     "timing": "host wall clock, one graph per step, no flush"}
         if looped:

@@ -113,6 +113,8 @@ SIGNATURES = {
     "fs_batch_get_stats": (C.c_int, [_P, C.POINTER(fs_stats)]),
     "fs_batch_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "fs_autotune": (C.c_int, [C.POINTER(fs_config), _F, _F, _F, _I, C.c_char_p, C.POINTER(C.c_double)]),
+    "fs_batch_autotune": (C.c_int, [C.POINTER(fs_config), _I, C.POINTER(_I), C.POINTER(_I), _F, _F, _F, _I,
+                                    C.c_char_p, C.POINTER(C.c_double)]),
     "fs_conv_pack_weights": (C.c_int, [_P, _P, _P]),
     "fs_conv3x3": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P]),
     "fs_net_avgpool2": (C.c_int, [_P, _P, _I, _I, _P]),
@@ -195,6 +197,21 @@ def autotune(rows, cols, diffusion_rate, viscosity, dt, steps=5, cache_path=None
     ms = C.c_double()
     path = str(cache_path).encode() if cache_path else None
     _check(L.fs_autotune(C.byref(cfg), diffusion_rate, viscosity, dt, steps, path, C.byref(ms)))
+    return {"tile_rows": cfg.tile_rows, "sweeps_per_pass": cfg.sweeps_per_pass, "ms_per_step": ms.value}
+
+
+def autotune_batch(shapes, diffusion_rate, viscosity, dt, steps=3, cache_path=None, **config) -> dict:
+    """Pick tile_rows / sweeps_per_pass for a batch of grids of these (rows, cols) shapes
+    by timing whole batch steps on the device (fs_batch_autotune). Returns the chosen
+    fields and the time per step."""
+    L = load()
+    cfg = default_config(3, 3, **config)
+    n = len(shapes)
+    rows = (C.c_int * n)(*[int(r) for r, _ in shapes])
+    cols = (C.c_int * n)(*[int(c) for _, c in shapes])
+    ms = C.c_double()
+    path = str(cache_path).encode() if cache_path else None
+    _check(L.fs_batch_autotune(C.byref(cfg), n, rows, cols, diffusion_rate, viscosity, dt, steps, path, C.byref(ms)))
     return {"tile_rows": cfg.tile_rows, "sweeps_per_pass": cfg.sweeps_per_pass, "ms_per_step": ms.value}
 
 

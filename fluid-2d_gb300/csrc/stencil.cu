@@ -1129,9 +1129,9 @@ __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
 // of them, with their descriptors in the launch's parameters like the single-grid
 // kernel's: one CTA per tile of the concatenated tile list, the tile's field found by a
 // binary search of the fields' first tiles. No global load precedes the tile's own.
-// (A device-resident descriptor table, fetched and staged in shared memory by each CTA,
-// made the batch's pressure passes 20-55 % slower than the same grid's single-grid
-// passes.)
+// (The previous form, a device-resident descriptor table that each CTA fetched into
+// shared memory, with masked direct loads for edge tiles, made the batch's pressure
+// passes 20-55 % slower than the same grid's single-grid passes.)
 template <int TY, int SRB, bool DIFF>
 __global__ void __launch_bounds__(kRegionW* TY, (TY <= 2 ? 2 : 1))
     stencil_wide_kernel(const __grid_constant__ WideLaunch L) {

@@ -263,6 +263,16 @@ FS_API int fs_stage(fs_solver* s, int stage, float rate, float dt);
 FS_API int fs_autotune(fs_config* cfg, float diffusion_rate, float viscosity, float dt, int steps,
                        const char* cache_path, double* best_ms);
 
+/* Autotuner for batches: the same search (region heights 64 and 128; depths 2, 4, ..., 16
+ * and those that split cfg->pressure_iterations into two, three or four equal passes)
+ * over whole steps of a batch of `count` grids of rows[k] x cols[k], each on a smooth
+ * divergent tuning state, `steps` timed steps after one warm-up step per candidate; the
+ * fastest goes into cfg->tile_rows / cfg->sweeps_per_pass for fs_batch_create. With
+ * cache_path the choice is looked up first and stored after tuning (key: device, SM
+ * count, a hash of the shapes, kd, kp). No counterpart in the reference. */
+FS_API int fs_batch_autotune(fs_config* cfg, int count, const int* rows, const int* cols, float diffusion_rate,
+                             float viscosity, float dt, int steps, const char* cache_path, double* best_ms);
+
 /* Batches: many independent grids of uneven size advanced together. No counterpart
  * in the reference (which steps one grid per fluid_solver_gpu object). Every sub-step
  * of the step is one launch over all grids; the step is replayed as a CUDA graph.

@@ -27,6 +27,31 @@ def test_autotune_picks_caches_and_keeps_parity(fluid, wl, tmp_path):
         assert oracle.rel_linf(g, o) <= 1e-5
 
 
+def test_batch_autotune_picks_caches_and_keeps_parity(fluid, wl, tmp_path):
+    shapes = [(34, 34), (66, 40), (130, 130), (5, 5), (17, 120)]
+    ins = [wl.random_state(r, c, 300 + k, vmax=0.03) for k, (r, c) in enumerate(shapes)]
+    cache = tmp_path / "tune_batch.txt"
+    kw = dict(diffuse_iterations=20, pressure_iterations=30, device=0)
+    t1 = fluid.autotune_batch(shapes, 1e-3, 1e-3, 0.05, steps=1, cache_path=cache, **kw)
+    # depths 2..16 and 15, 10, 8 (30 pressure sweeps in two, three or four passes)
+    assert t1["tile_rows"] in (64, 128) and 2 <= t1["sweeps_per_pass"] <= 16 and t1["ms_per_step"] > 0
+    lines = cache.read_text().strip().splitlines()
+    assert len(lines) == 1 and lines[0].split()[1:3] == [str(t1["tile_rows"]), str(t1["sweeps_per_pass"])]
+    t2 = fluid.autotune_batch(shapes, 1e-3, 1e-3, 0.05, steps=1, cache_path=cache, **kw)
+    assert (t2["tile_rows"], t2["sweeps_per_pass"]) == (t1["tile_rows"], t1["sweeps_per_pass"])
+    assert len(cache.read_text().strip().splitlines()) == 1  # served from the cache
+    with fluid.Batch(shapes, tile_rows=t1["tile_rows"], sweeps_per_pass=t1["sweeps_per_pass"], **kw) as b:
+        for k, (d, u, v, ds, us, vs) in enumerate(ins):
+            b.upload(k, d, u, v)
+            b.upload_sources(k, ds, us, vs)
+        b.step(1e-3, 1e-3, 0.05, nsteps=2)
+        got = [b.download(k) for k in range(len(shapes))]
+    for k, (d, u, v, ds, us, vs) in enumerate(ins):
+        want = oracle.gpu_solve(d, ds, 1e-3, u, v, us, vs, 1e-3, 0.05, kd=20, kp=30, nsteps=2)
+        for g, o in zip(got[k], want):
+            assert oracle.rel_linf(g, o) <= 1e-5, shapes[k]
+
+
 def test_default_depth_rule(fluid):
     """sweeps_per_pass = 0: depth 8 on large grids and residual-target solves; the fewest
     passes on launch-bound small grids; an explicit depth is kept."""
