@@ -57,8 +57,9 @@ struct fs_batch {
     bool graph_valid = false;
     float g_diff = 0, g_visc = 0, g_dt = 0;
     int sweeps = 8, tile_rows = 64;
-    // host-built plan, mirrored in one device buffer
-    std::vector<WideLaunch> h_wide;  // stencil launches (descriptors travel as parameters)
+    // host-built plan: the stencil launches (their descriptors travel as parameters) and
+    // the advection job tables, which are mirrored in one device buffer
+    std::vector<WideLaunch> h_wide;
     std::vector<AdvectJob> h_jobs;
     std::vector<int> h_jprefix;
     std::vector<int> h_map;   // block -> job for every advection op
@@ -263,7 +264,7 @@ int build_plan(fs_batch* b, float diff, float visc, float dt) {
             L.job_blocks[op] = blocks;
         }
     }
-    // ---- upload (one buffer, tables first)
+    // ---- upload the job tables (one buffer)
     const size_t job_bytes = b->h_jobs.size() * sizeof(AdvectJob);
     const size_t jpre_bytes = b->h_jprefix.size() * sizeof(int);
     const size_t map_bytes = b->h_map.size() * sizeof(int);
