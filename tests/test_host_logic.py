@@ -70,3 +70,17 @@ def test_drag_script_is_seeded_sorted_and_inside(wl):
         assert 1 <= i <= 64 and 1 <= j <= 78 and kind in (0, 1)
         if kind == 1:
             assert abs(np.hypot(x, y) - 0.05) < 1e-6
+
+
+def test_batch_workload_sizes(wl):
+    """The batch workload draws its seeded sizes from 64..1024 in steps of 64, or takes
+    explicit interior sizes (bench.py --batch-sizes), one grid each, boundary added."""
+    drawn = wl.batch_sizes(256, seed=4)
+    assert len(drawn) == 256 and set(drawn) <= set(range(64, 1025, 64))
+    assert drawn == wl.batch_sizes(256, seed=4)
+    sims = wl.batch(sizes=[64, 30], kd=30, kp=30)
+    assert [(w.rows, w.cols) for w in sims] == [(66, 66), (32, 32)]
+    for w in sims:
+        d, u, v = w.state()
+        assert d.dtype == np.float32 and d.shape == (w.rows, w.cols)
+        assert np.isfinite(u).all() and np.isfinite(v).all()
